@@ -1,0 +1,439 @@
+// C ABI: contexts, resident graphs, counting.
+//
+// A count follows occurrences() (src/fringeCount.cu:2199-2262): vertex and edge
+// cores return their raw total; larger cores divide it by the pattern's count
+// in itself, computed with the same kernels on the pattern graph built from the
+// matching order (matchingOrder2ECLgraph, :121-186) and cached per pattern.
+// Unlike the reference, all device state lives in the context (no file-scope
+// device globals), so any number of counts and contexts can coexist.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fsgc_internal.h"
+
+using fsgc::DevGraph;
+typedef unsigned long long u64;
+
+struct fsgc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string err;
+  uint64_t launches = 0;
+  std::map<int, DevGraph*> graphs;
+  int next_gid = 1;
+  fsgc::DevWork work;
+  u64* d_slots = nullptr;
+  u64* h_slots = nullptr;
+  int slot_cap = 0;
+  std::vector<cudaEvent_t> events;
+  std::map<std::string, u64> aut_cache;
+};
+
+namespace {
+
+std::mutex g_init_mu;
+bool g_magic_uploaded[64] = {false};
+
+int fail(fsgc_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+int cuda_fail(fsgc_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, e == cudaErrorMemoryAllocation ? FSGC_ENOMEM : FSGC_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                              \
+  do {                                              \
+    cudaError_t e__ = (expr);                       \
+    if (e__ != cudaSuccess) return cuda_fail(c, e__, what); \
+  } while (0)
+
+void free_graph(DevGraph* g) {
+  if (!g) return;
+  cudaFree(g->off);
+  cudaFree(g->adj);
+  cudaFree(g->deg);
+  cudaFree(g->ooff);
+  cudaFree(g->oadj);
+  cudaFree(g->osrc);
+  cudaFree(g->osup);
+  cudaFree(g->vtri2);
+  delete g;
+}
+
+int ensure_slots(fsgc_ctx* c, int n) {
+  if (n <= c->slot_cap) return FSGC_OK;
+  int cap = std::max(n, 2 * c->slot_cap);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->d_slots);
+  cudaFreeHost(c->h_slots);
+  c->d_slots = nullptr;
+  c->h_slots = nullptr;
+  CK(cudaMalloc((void**)&c->d_slots, sizeof(u64) * (size_t)cap), "slot allocation");
+  CK(cudaMallocHost((void**)&c->h_slots, sizeof(u64) * (size_t)cap), "slot allocation");
+  c->slot_cap = cap;
+  return FSGC_OK;
+}
+
+int ensure_events(fsgc_ctx* c, size_t n) {
+  while (c->events.size() < n) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e), "event creation");
+    c->events.push_back(e);
+  }
+  return FSGC_OK;
+}
+
+// Upload a host CSR (64-bit offsets) as a new DevGraph.
+int upload_graph(fsgc_ctx* c, int n, long long m, const long long* off, const int* adj, bool device_src,
+                 DevGraph** out) {
+  DevGraph* g = new DevGraph();
+  g->n = n;
+  g->m = m;
+  cudaError_t e = cudaMalloc((void**)&g->off, sizeof(long long) * ((size_t)n + 1));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&g->adj, sizeof(int) * (size_t)std::max(1LL, m));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&g->deg, sizeof(int) * (size_t)std::max(1, n));
+  if (e != cudaSuccess) {
+    free_graph(g);
+    cudaGetLastError();
+    return cuda_fail(c, e, "graph allocation");
+  }
+  const cudaMemcpyKind kind = device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  e = cudaMemcpyAsync(g->off, off, sizeof(long long) * ((size_t)n + 1), kind, c->stream);
+  if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(g->adj, adj, sizeof(int) * (size_t)m, kind, c->stream);
+  if (e != cudaSuccess) {
+    free_graph(g);
+    return cuda_fail(c, e, "graph upload");
+  }
+  g->bytes = sizeof(long long) * ((size_t)n + 1) + sizeof(int) * ((size_t)m + (size_t)n);
+  *out = g;
+  return FSGC_OK;
+}
+
+// Pattern graph of a matching order (src/fringeCount.cu:121-186): core vertices
+// 0..k-1 joined as mo.list says, then each anchor set's fringes.
+void pattern_csr(const fsgc_matching_order& mo, std::vector<long long>& off, std::vector<int>& adj) {
+  int n = mo.nodes;
+  for (int i = 0; i < mo.anchorsets; i++) n += mo.fcnt[i];
+  std::vector<std::vector<int>> nb(n);
+  for (int i = 0; i < mo.nodes - 1; i++)
+    for (int j = 0; j <= i; j++)
+      if (mo.list[i] & (1 << j)) { nb[i + 1].push_back(j); nb[j].push_back(i + 1); }
+  int v = mo.nodes;
+  for (int i = 0; i < mo.anchorsets; i++)
+    for (int t = 0; t < mo.fcnt[i]; t++, v++)
+      for (int j = 0; j < FSGC_MAX_CORE; j++)
+        if (mo.anch[i] & (1 << j)) { nb[j].push_back(v); nb[v].push_back(j); }
+  off.assign((size_t)n + 1, 0);
+  adj.clear();
+  for (int x = 0; x < n; x++) {
+    std::sort(nb[x].begin(), nb[x].end());
+    adj.insert(adj.end(), nb[x].begin(), nb[x].end());
+    off[x + 1] = (long long)adj.size();
+  }
+}
+
+bool mo_valid(const fsgc_matching_order& mo) {
+  if (mo.nodes < 1 || mo.nodes > FSGC_MAX_CORE || mo.anchorsets > 63) return false;
+  int total = mo.nodes;
+  for (int i = 0; i < mo.anchorsets; i++) {
+    if (mo.anch[i] == 0 || mo.anch[i] >= (1 << mo.nodes)) return false;
+    total += mo.fcnt[i];
+  }
+  for (int i = 0; i + 1 < mo.nodes; i++)
+    if (mo.list[i] == 0 || mo.list[i] >= (2 << i)) return false;
+  return total <= FSGC_MAX_PATTERN;
+}
+
+// The divisor for cores of 3+ vertices: the pattern counted in itself with the
+// same kernels.  The reference stores it in an int (src/fringeCount.cu:2213).
+int automorphisms(fsgc_ctx* c, const fsgc_matching_order& mo, u64* out) {
+  const std::string key(reinterpret_cast<const char*>(&mo), sizeof(mo));
+  auto it = c->aut_cache.find(key);
+  if (it != c->aut_cache.end()) {
+    *out = it->second;
+    return FSGC_OK;
+  }
+  std::vector<long long> off;
+  std::vector<int> adj;
+  pattern_csr(mo, off, adj);
+  const int pn = (int)off.size() - 1;
+  DevGraph* pg = nullptr;
+  int st = upload_graph(c, pn, off[pn], off.data(), adj.data(), false, &pg);
+  if (st != FSGC_OK) return st;
+  st = ensure_slots(c, 1);
+  if (st != FSGC_OK) { free_graph(pg); return st; }
+  cudaMemsetAsync(c->d_slots, 0, sizeof(u64), c->stream);
+  fsgc::CountJob job{&mo, pg, c->d_slots, 0, 0, false};
+  st = fsgc::enqueue_count(job, c->stream, &c->launches, c->work);
+  u64 raw = 0;
+  if (st == FSGC_OK) {
+    if (job.host_only) raw = job.host_value;
+    else {
+      cudaMemcpyAsync(c->h_slots, c->d_slots, sizeof(u64), cudaMemcpyDeviceToHost, c->stream);
+      cudaError_t e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) st = cuda_fail(c, e, "automorphism count");
+      raw = c->h_slots[0];
+    }
+  } else {
+    fail(c, st, "automorphism count failed (%d)", st);
+  }
+  cudaStreamSynchronize(c->stream);
+  free_graph(pg);
+  if (st != FSGC_OK) return st;
+  const u64 aut = (u64)(unsigned int)(int)raw;
+  if (aut == 0) return fail(c, FSGC_EINVAL, "pattern has no match in itself");
+  c->aut_cache[key] = aut;
+  *out = aut;
+  return FSGC_OK;
+}
+
+// Size check of occurrences() (src/fringeCount.cu:2216-2219).
+bool pattern_too_large(const fsgc_matching_order& mo, const DevGraph& g) {
+  if (mo.nodes < 3) return false;
+  long long pn = mo.nodes, pm = 0;
+  for (int i = 0; i + 1 < mo.nodes; i++) pm += 2 * __builtin_popcount(mo.list[i]);
+  for (int i = 0; i < mo.anchorsets; i++) {
+    pn += mo.fcnt[i];
+    pm += 2LL * mo.fcnt[i] * __builtin_popcount(mo.anch[i]);
+  }
+  return pn > g.n || pm > g.m;
+}
+
+DevGraph* find_graph(fsgc_ctx* c, int gid) {
+  auto it = c->graphs.find(gid);
+  return it == c->graphs.end() ? nullptr : it->second;
+}
+
+int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
+  if (nt <= 0) return FSGC_OK;
+  int st = ensure_slots(c, nt);
+  if (st != FSGC_OK) return st;
+  st = ensure_events(c, (size_t)nt + 1);
+  if (st != FSGC_OK) return st;
+  std::vector<u64> aut((size_t)nt, 1);
+  std::vector<fsgc::CountJob> jobs((size_t)nt);
+  for (int t = 0; t < nt; t++) {
+    const fsgc_matching_order& mo = tasks[t].mo;
+    memset(&res[t], 0, sizeof(fsgc_result));
+    if (!mo_valid(mo)) return fail(c, FSGC_EINVAL, "task %d: malformed matching order", t);
+    DevGraph* g = find_graph(c, tasks[t].gid);
+    if (!g) return fail(c, FSGC_ENOTFOUND, "task %d: unknown graph %d", t, tasks[t].gid);
+    if (mo.nodes >= 3 && !pattern_too_large(mo, *g)) {
+      st = automorphisms(c, mo, &aut[t]);
+      if (st != FSGC_OK) return st;
+    }
+  }
+  CK(cudaMemsetAsync(c->d_slots, 0, sizeof(u64) * (size_t)nt, c->stream), "slot reset");
+  CK(cudaEventRecord(c->events[0], c->stream), "event");
+  for (int t = 0; t < nt; t++) {
+    const fsgc_matching_order& mo = tasks[t].mo;
+    DevGraph* g = find_graph(c, tasks[t].gid);
+    jobs[t] = fsgc::CountJob{&tasks[t].mo, g, c->d_slots + t, 0, 0, false};
+    if (pattern_too_large(mo, *g)) {
+      jobs[t].host_only = true;
+      jobs[t].host_value = 0;
+      jobs[t].core_type = (mo.nodes == 3) ? ((__builtin_popcount(mo.list[1]) == 1) ? FSGC_CORE_WEDGE : FSGC_CORE_TRIANGLE)
+                                          : FSGC_CORE_GENERAL;
+      res[t].flags |= FSGC_FLAG_PATTERN_TOO_LARGE;
+    } else {
+      st = fsgc::enqueue_count(jobs[t], c->stream, &c->launches, c->work);
+      if (st != FSGC_OK) {
+        cudaStreamSynchronize(c->stream);
+        return fail(c, st, "task %d: count failed (%s)", t, cudaGetErrorString(cudaGetLastError()));
+      }
+    }
+    CK(cudaEventRecord(c->events[t + 1], c->stream), "event");
+  }
+  CK(cudaMemcpyAsync(c->h_slots, c->d_slots, sizeof(u64) * (size_t)nt, cudaMemcpyDeviceToHost, c->stream), "readback");
+  CK(cudaStreamSynchronize(c->stream), "count");
+  for (int t = 0; t < nt; t++) {
+    const u64 raw = jobs[t].host_only ? jobs[t].host_value : c->h_slots[t];
+    res[t].raw_total = raw;
+    res[t].automorphisms = aut[t];
+    res[t].count = raw / aut[t];
+    res[t].core_type = jobs[t].core_type;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->events[t], c->events[t + 1]);
+    res[t].device_ms = ms;
+  }
+  return FSGC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fsgc_ctx_create(int device, fsgc_ctx** out) {
+  if (!out) return FSGC_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return FSGC_ENODEV;
+  }
+  if (device < 0 || device >= ndev) return FSGC_EINVAL;
+  if (cudaSetDevice(device) != cudaSuccess) return FSGC_ECUDA;
+  fsgc_ctx* c = new fsgc_ctx();
+  c->device = device;
+  {
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (device < 64 && !g_magic_uploaded[device]) {
+      fsgc::upload_div_magic();
+      g_magic_uploaded[device] = true;
+    }
+  }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc((void**)&c->work.small, 32 * sizeof(u64)) != cudaSuccess || ensure_slots(c, 64) != FSGC_OK) {
+    cudaGetLastError();
+    fsgc_ctx_destroy(c);
+    return FSGC_ECUDA;
+  }
+  cudaMemset(c->work.small, 0, 32 * sizeof(u64));
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    // kernels for this architecture missing or device unusable
+    cudaGetLastError();
+    fsgc_ctx_destroy(c);
+    return FSGC_ENODEV;
+  }
+  *out = c;
+  return FSGC_OK;
+}
+
+void fsgc_ctx_destroy(fsgc_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->graphs) free_graph(kv.second);
+  c->graphs.clear();
+  for (auto e : c->events) cudaEventDestroy(e);
+  cudaFree(c->work.small);
+  cudaFree(c->work.pairs.ptr);
+  cudaFree(c->d_slots);
+  cudaFreeHost(c->h_slots);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* fsgc_ctx_last_error(const fsgc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+void* fsgc_ctx_stream(fsgc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+uint64_t fsgc_ctx_launches(const fsgc_ctx* c) { return c ? c->launches : 0; }
+
+int fsgc_graph_from_csr(fsgc_ctx* c, int n, int64_t m, const int64_t* nindex, const int32_t* nlist, int* gid) {
+  if (!c || !gid || n < 1 || m < 0 || !nindex || (m > 0 && !nlist)) return fail(c, FSGC_EINVAL, "bad graph arguments");
+  if (nindex[0] != 0 || nindex[n] != m) return fail(c, FSGC_EINVAL, "offsets must start at 0 and end at m");
+  for (int v = 0; v < n; v++)
+    if (nindex[v + 1] < nindex[v]) return fail(c, FSGC_EINVAL, "offsets decrease at vertex %d", v);
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DevGraph* g = nullptr;
+  int st = upload_graph(c, n, m, (const long long*)nindex, nlist, false, &g);
+  if (st != FSGC_OK) return st;
+  *gid = c->next_gid++;
+  c->graphs[*gid] = g;
+  return FSGC_OK;
+}
+
+int fsgc_graph_from_csr32(fsgc_ctx* c, int n, int m, const int32_t* nindex, const int32_t* nlist, int* gid) {
+  if (!c || n < 1 || m < 0 || !nindex) return fail(c, FSGC_EINVAL, "bad graph arguments");
+  std::vector<int64_t> off((size_t)n + 1);
+  for (int v = 0; v <= n; v++) off[v] = nindex[v];
+  return fsgc_graph_from_csr(c, n, m, off.data(), nlist, gid);
+}
+
+int fsgc_graph_from_device_csr(fsgc_ctx* c, int n, int64_t m, const int64_t* d_nindex, const int32_t* d_nlist,
+                               int* gid) {
+  if (!c || !gid || n < 1 || m < 0 || !d_nindex || (m > 0 && !d_nlist)) return fail(c, FSGC_EINVAL, "bad graph arguments");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DevGraph* g = nullptr;
+  int st = upload_graph(c, n, m, (const long long*)d_nindex, d_nlist, true, &g);
+  if (st != FSGC_OK) return st;
+  *gid = c->next_gid++;
+  c->graphs[*gid] = g;
+  return FSGC_OK;
+}
+
+int fsgc_graph_load_egr(fsgc_ctx* c, const char* path, int* gid) {
+  fsgc_host_csr h;
+  const int st = fsgc_egr_read(path, &h);
+  if (st != FSGC_OK) return fail(c, st, "could not read graph file %s", path ? path : "(null)");
+  const int r = fsgc_graph_from_csr(c, h.n, h.m, h.nindex, h.nlist, gid);
+  if (c) cudaStreamSynchronize(c->stream);
+  fsgc_host_csr_free(&h);
+  return r;
+}
+
+int fsgc_graph_release(fsgc_ctx* c, int gid) {
+  if (!c) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  auto it = c->graphs.find(gid);
+  if (it == c->graphs.end()) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", gid);
+  cudaStreamSynchronize(c->stream);
+  free_graph(it->second);
+  c->graphs.erase(it);
+  return FSGC_OK;
+}
+
+int fsgc_graph_info_get(fsgc_ctx* c, int gid, fsgc_graph_info* out) {
+  if (!c || !out) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DevGraph* g = find_graph(c, gid);
+  if (!g) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", gid);
+  out->n = g->n;
+  out->m = g->m;
+  out->max_degree = g->maxdeg;
+  out->triangles = g->prepared ? g->triangles : -1;
+  out->device_bytes = (int64_t)g->bytes;
+  return FSGC_OK;
+}
+
+int fsgc_count(fsgc_ctx* c, int gid, const fsgc_matching_order* mo, fsgc_result* out) {
+  if (!c || !mo || !out) return fail(c, FSGC_EINVAL, "null argument");
+  fsgc_task t;
+  t.gid = gid;
+  t.mo = *mo;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  return count_tasks(c, &t, 1, out);
+}
+
+int fsgc_count_batch(fsgc_ctx* c, const fsgc_task* tasks, int ntasks, fsgc_result* results) {
+  if (!c || ntasks < 0 || (ntasks > 0 && (!tasks || !results))) return fail(c, FSGC_EINVAL, "bad batch arguments");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  return count_tasks(c, tasks, ntasks, results);
+}
+
+// Host evaluation of the device binomial (same magic-number division) so that
+// the arithmetic can be checked without a GPU.
+unsigned long long fsgc_nck_host(int n, int k) {
+  static fsgc::DivMagic tab[fsgc::kMaxDiv];
+  static bool init = false;
+  if (!init) {
+    for (int d = 2; d < fsgc::kMaxDiv; d++) tab[d] = fsgc::make_div_magic((unsigned)d);
+    init = true;
+  }
+  return fsgc::nck_ref(n, k, tab);
+}
+
+unsigned long long fsgc_div_small_host(unsigned long long x, unsigned d) {
+  if (d < 2 || d >= (unsigned)fsgc::kMaxDiv) return 0;
+  return fsgc::div_magic(x, fsgc::make_div_magic(d));
+}
+
+}  // extern "C"

@@ -1,0 +1,899 @@
+// Counting kernels: one family per core shape of the matching order.
+//
+// Every kernel evaluates, per core match, the reference's closed-form fringe
+// count with the reference's u64 arithmetic (nck_ref) and the reference's
+// vertex roles, and adds it into a u64 result slot through a warp -> block ->
+// slot reduction.  The per-match formulas are fixed by the reference; what
+// changes is how the matches and their Venn sizes are found:
+//   vertex core   one pass over the degrees;
+//   edge core     one pass over oriented edges, common-neighbour counts taken
+//                 from the loader's per-edge triangle supports;
+//   triangle core triangles enumerated once on the oriented graph, pairwise
+//                 overlaps from the supports, the triple overlap by a
+//                 warp-cooperative intersection over the smallest list;
+//   wedge core    (centre without fringes) aggregated per endpoint pair: the
+//                 reference evaluates the same formula once per centre, and
+//                 the formula does not depend on the centre, so each pair is
+//                 evaluated once and multiplied by its number of centres;
+//                 (centre with fringes) one warp per centre-endpoint edge;
+//   general core  warp-cooperative depth-first matching of 4-6 core vertices,
+//                 a Venn histogram per match and a per-lane placement sum.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "fsgc_internal.h"
+
+namespace fsgc {
+
+__constant__ DivMagic c_div[kMaxDiv];
+
+void upload_div_magic() {
+  DivMagic t[kMaxDiv];
+  t[0] = DivMagic{0, 1};
+  t[1] = DivMagic{0, 1};
+  for (int d = 2; d < kMaxDiv; d++) t[d] = make_div_magic((unsigned)d);
+  cudaMemcpyToSymbol(c_div, t, sizeof(t));
+}
+
+namespace {
+
+constexpr int kTPB = 256;
+enum { IU = 1, IV = 2, IW = 4, IUV = 3, IUW = 5, IVW = 6, IUVW = 7 };
+
+__device__ __forceinline__ u64 nck(int n, int k) { return nck_ref(n, k, c_div); }
+
+// ------------------------------------------------------------- shared formulas
+// Edge-core formula (src/fringeCount.cu:2030-2049) for an edge (u, v), where
+// u is the endpoint with the larger vertex id and c_uv = |N(u) & N(v)|.
+__device__ u64 edge_formula(int du, int dv, int c_uv, int f_u, int f_uv, int f_v) {
+  const int a_uv = c_uv - f_uv;
+  if (a_uv < 0) return 0;
+  const int c_u = du - 1 - c_uv, c_v = dv - 1 - c_uv;
+  const int bound = min(f_u, a_uv);
+  u64 acc = 0;
+  for (int j = 0; j <= bound; j++) {
+    const int k = f_u - j;
+    u64 term = nck(c_u, k) * nck(a_uv + c_v - j, f_v);
+    if (f_u != f_v) term += nck(c_v, k) * nck(a_uv + c_u - j, f_v);
+    acc += term * nck(a_uv, j);
+  }
+  return acc * nck(c_uv, f_uv);
+}
+
+// wedge() (src/fringeCount.cu:1381-1406): endpoints x (larger id) and y of a
+// wedge; c = common neighbours of x and y other than the centre.
+__device__ u64 wedge_formula(int dx, int dy, bool adj, int f_x, int f_xy, int f_y, int c) {
+  const int a_xy = c - f_xy;
+  if (a_xy < 0) return 0;
+  const int corr = adj ? 2 : 1;
+  const int a_x = dx - (corr + c), a_y = dy - (corr + c);
+  const int bound = min(f_x, a_xy);
+  u64 sum = 0;
+  for (int j = 0; j <= bound; j++) {
+    const int k = f_x - j;
+    u64 term = nck(a_x, k) * nck(a_xy + a_y - j, f_y);
+    if (f_x != f_y) term += nck(a_y, k) * nck(a_xy + a_x - j, f_y);
+    sum += term * nck(a_xy, j);
+  }
+  return sum * nck(c, f_xy);
+}
+
+// fc3 (src/fringeCount.cu:233-327): placements of the seven anchor-set types of
+// a 3-vertex core into its seven exclusive Venn regions.  Same summation
+// indices and the same nck factors per term as the reference.
+__device__ u64 fc3(const int* fr, const int* venn) {
+  const int fuvw = fr[IUVW], fuv = fr[IUV], fuw = fr[IUW], fvw = fr[IVW];
+  const int fu = fr[IU], fv = fr[IV], fw = fr[IW];
+  int x_uvw = venn[IUVW];
+  const int x_uv = venn[IUV], x_uw = venn[IUW], x_vw = venn[IVW];
+  const int x_u = venn[IU], x_v = venn[IV], x_w = venn[IW];
+  if (x_uvw < fuvw) return 0;
+  const u64 base = nck(x_uvw, fuvw);
+  x_uvw -= fuvw;
+  u64 total = 0;
+  for (int i = min(x_uvw, fuv); i >= 0; i--) {
+    if (x_uv < fuv - i) break;
+    const u64 t1 = base * nck(x_uvw, i) * nck(x_uv, fuv - i);
+    const int r1 = x_uvw - i, r_uv = x_uv - (fuv - i);
+    for (int j = min(r1, fuw); j >= 0; j--) {
+      if (x_uw < fuw - j) break;
+      const u64 t2 = t1 * nck(r1, j) * nck(x_uw, fuw - j);
+      const int r2 = r1 - j, r_uw = x_uw - (fuw - j);
+      for (int k = min(r2, fvw); k >= 0; k--) {
+        if (x_vw < fvw - k) break;
+        const u64 t3 = t2 * nck(r2, k) * nck(x_vw, fvw - k);
+        const int r3 = r2 - k, r_vw = x_vw - (fvw - k);
+        for (int a = min(r3, fu); a >= 0; a--) {
+          const u64 ta = t3 * nck(r3, a);
+          const int pool_v = (r3 - a) + r_vw;
+          for (int b = min(r_uv, fu - a); b >= 0; b--) {
+            const u64 tb = ta * nck(r_uv, b);
+            const int r_uv2 = r_uv - b;
+            for (int c = min(r_uw, fu - a - b); c >= 0; c--) {
+              if (x_u < fu - a - b - c) break;
+              const u64 tc = tb * nck(r_uw, c) * nck(x_u, fu - a - b - c);
+              const int r_uw2 = r_uw - c;
+              for (int d = min(pool_v, fv); d >= 0; d--) {
+                if (r_uv2 + x_v < fv - d) break;
+                const u64 td = tc * nck(pool_v, d) * nck(r_uv2 + x_v, fv - d);
+                const int pool_w = (pool_v - d) + r_uw2 + x_w;
+                if (pool_w >= fw) total += td * nck(pool_w, fw);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  return total;
+}
+
+struct Rot3 {
+  int fr[6][8];
+  int count;
+};
+
+// ------------------------------------------------------------- vertex core
+__global__ void star_kernel(GView g, int t, u64* __restrict__ slot) {
+  u64 acc = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x) {
+    const int d = g.deg[v];
+    if (d >= t) acc += nck(d, t);
+  }
+  block_sum_to(acc, slot);
+}
+
+// ------------------------------------------------------------- edge core
+struct EdgeParams {
+  int f_u, f_uv, f_v, lim1, lim2;
+};
+
+__global__ void edge_kernel(GView g, EdgeParams p, u64* __restrict__ slot) {
+  const long long me = g.m / 2;
+  u64 acc = 0;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < me; j += (long long)gridDim.x * blockDim.x) {
+    const int a = g.osrc[j], b = g.oadj[j];
+    const int u = max(a, b), v = min(a, b);  // the reference orients by id, v < u
+    const int du = g.deg[u], dv = g.deg[v];
+    if (!(du > p.lim1 && dv > p.lim1 && du + dv > p.lim2)) continue;  // init_wl_edge pruning
+    acc += edge_formula(du, dv, (int)g.osup[j], p.f_u, p.f_uv, p.f_v);
+  }
+  block_sum_to(acc, slot);
+}
+
+// triangle with `tails` fringes on one vertex: sum over triangles of the three
+// vertex terms = sum over vertices of (triangles at v) * C(deg v - 2, tails)
+__global__ void tailed_triangle_kernel(GView g, const u64* __restrict__ vtri2, int tails, u64* __restrict__ slot) {
+  u64 acc = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x) {
+    const u64 t2 = vtri2[v];
+    if (t2) acc += (t2 >> 1) * nck(g.deg[v] - 2, tails);
+  }
+  block_sum_to(acc, slot);
+}
+
+// ------------------------------------------------------------- triangle core
+struct TriParams {
+  int sum1, sum2, sum3;
+  int mode;   // 0 general, 1 4-clique, 2 tailed 4-clique
+  int tails;
+  int relabel;  // roles by (deg, id) order (1) or by id (0)
+  Rot3 rot;
+};
+
+// Merge step over two sorted out-lists: advance (i,k) to the next common element.
+__device__ __forceinline__ bool next_common(const int* A, int la, const int* B, int lb, int& i, int& k) {
+  while (i < la && k < lb) {
+    const int x = __ldg(A + i), y = __ldg(B + k);
+    if (x < y) i++;
+    else if (y < x) k++;
+    else return true;
+  }
+  return false;
+}
+
+// warp-cooperative |L0 & L1 & L2| for three sorted lists, iterating the shortest
+__device__ int warp_triple(const int* L0, int l0, const int* L1, int l1, const int* L2, int l2) {
+  const int lane = threadIdx.x & 31;
+  // put the shortest list first
+  if (l1 < l0) { const int* t = L0; L0 = L1; L1 = t; int tl = l0; l0 = l1; l1 = tl; }
+  if (l2 < l0) { const int* t = L0; L0 = L2; L2 = t; int tl = l0; l0 = l2; l2 = tl; }
+  int c = 0;
+  for (int i = lane; i < l0; i += 32) {
+    const int x = __ldg(L0 + i);
+    if (bsearch_has(L1, l1, x) && bsearch_has(L2, l2, x)) c++;
+  }
+  return __reduce_add_sync(0xffffffffu, c);
+}
+
+__device__ __forceinline__ long long tri_key(int x, int d, int relabel) {
+  // larger key = later in the reference's vertex order (its new ids ascend
+  // with descending (deg, id) after the relabel, with the id otherwise)
+  return relabel ? -(((long long)d << 32) | (unsigned)x) : (long long)x;
+}
+
+// One lane per oriented edge (a -> b); triangles a < b < c are found by merging
+// the out-lists.  Found triangles are served one at a time by the whole warp.
+__global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slot) {
+  const int lane = threadIdx.x & 31;
+  const long long me = g.m / 2;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  u64 acc = 0;
+  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x - lane); base < me; base += nwarps * 32) {
+    const long long j = base + lane;
+    bool live = j < me;
+    int a = 0, b = 0, la = 0, lb = 0, i = 0, k = 0;
+    const int *A = nullptr, *B = nullptr;
+    long long aoff = 0, boff = 0;
+    if (live) {
+      a = g.osrc[j];
+      b = g.oadj[j];
+      aoff = g.ooff[a];
+      boff = g.ooff[b];
+      la = (int)(g.ooff[a + 1] - aoff);
+      lb = (int)(g.ooff[b + 1] - boff);
+      A = g.oadj + aoff;
+      B = g.oadj + boff;
+    }
+    while (__any_sync(0xffffffffu, live)) {
+      bool found = false;
+      int c = 0;
+      if (live) {
+        found = next_common(A, la, B, lb, i, k);
+        if (!found) live = false;
+        else c = A[i];
+      }
+      if (p.mode != 0) {
+        // 4-cliques a < b < c < d: d in out(a) & out(b) & out(c)
+        if (found) {
+          const long long coff = g.ooff[c];
+          const int lc = (int)(g.ooff[c + 1] - coff);
+          const int* C = g.oadj + coff;
+          for (int t = 0; t < lc; t++) {
+            const int d = __ldg(C + t);
+            if (bsearch_has(A, la, d) && bsearch_has(B, lb, d)) {
+              if (p.mode == 1) acc += 1;
+              else acc += nck(g.deg[a] - 3, p.tails) + nck(g.deg[b] - 3, p.tails) + nck(g.deg[c] - 3, p.tails) +
+                          nck(g.deg[d] - 3, p.tails);
+            }
+          }
+        }
+      } else {
+        // roles: u latest, w earliest in the reference's vertex order
+        int x[3], dx[3];
+        unsigned sx[3];  // support of the edge opposite... indexed by vertex pair below
+        int venn[8];
+        bool take = false;
+        if (found) {
+          x[0] = a; x[1] = b; x[2] = c;
+          dx[0] = g.deg[a]; dx[1] = g.deg[b]; dx[2] = g.deg[c];
+          // supports of edges ab, ac, bc
+          const unsigned s_ab = g.osup[j], s_ac = g.osup[aoff + i], s_bc = g.osup[boff + k];
+          // sort the three vertices by key descending: u, v, w
+          long long kx[3] = {tri_key(a, dx[0], p.relabel), tri_key(b, dx[1], p.relabel), tri_key(c, dx[2], p.relabel)};
+          int ord[3] = {0, 1, 2};
+          if (kx[ord[0]] < kx[ord[1]]) { int t = ord[0]; ord[0] = ord[1]; ord[1] = t; }
+          if (kx[ord[1]] < kx[ord[2]]) { int t = ord[1]; ord[1] = ord[2]; ord[2] = t; }
+          if (kx[ord[0]] < kx[ord[1]]) { int t = ord[0]; ord[0] = ord[1]; ord[1] = t; }
+          // pair support lookup
+          auto sup = [&](int p0, int p1) -> unsigned {
+            const int lo = min(p0, p1), hi = max(p0, p1);
+            return (lo == 0) ? (hi == 1 ? s_ab : s_ac) : s_bc;
+          };
+          const int iu = ord[0], iv = ord[1], iw = ord[2];
+          const int du = dx[iu], dv = dx[iv], dw = dx[iw];
+          // the reference's pruning (init_wl_triangle, common3_triangle)
+          const int th1 = max(p.sum1, p.sum2 - du);
+          const int th2 = max(max(p.sum1, p.sum3 - du - dv), max(p.sum2 - du, p.sum2 - dv));
+          take = (du >= p.sum1) && (dv >= th1) && (dw >= th2);
+          venn[IUV] = (int)sup(iu, iv);
+          venn[IUW] = (int)sup(iu, iw);
+          venn[IVW] = (int)sup(iv, iw);
+          venn[IU] = du; venn[IV] = dv; venn[IW] = dw;
+          sx[0] = x[iu]; sx[1] = x[iv]; sx[2] = x[iw];
+        }
+        // triple overlaps, one triangle at a time across the warp
+        unsigned bal = __ballot_sync(0xffffffffu, take);
+        int c123 = 0;
+        while (bal) {
+          const int who = __ffs(bal) - 1;
+          bal &= bal - 1;
+          const int q0 = __shfl_sync(0xffffffffu, (int)sx[0], who);
+          const int q1 = __shfl_sync(0xffffffffu, (int)sx[1], who);
+          const int q2 = __shfl_sync(0xffffffffu, (int)sx[2], who);
+          const long long o0 = g.off[q0], o1 = g.off[q1], o2 = g.off[q2];
+          const int r = warp_triple(g.adj + o0, (int)(g.off[q0 + 1] - o0), g.adj + o1, (int)(g.off[q1 + 1] - o1),
+                                    g.adj + o2, (int)(g.off[q2 + 1] - o2));
+          if (lane == who) c123 = r;
+        }
+        if (take) {
+          // com3 (src/fringeCount.cu:934-964): exclusive regions without the
+          // triangle's own vertices
+          const int p12 = venn[IUV], t13 = venn[IUW], t23 = venn[IVW];
+          const int c12 = p12 - (c123 + 1), c13 = t13 - (c123 + 1), c23 = t23 - (c123 + 1);
+          const int du = venn[IU], dv = venn[IV], dw = venn[IW];
+          venn[0] = 0;
+          venn[IU] = du - (c12 + c13 + (c123 + 2));
+          venn[IV] = dv - (c12 + c23 + (c123 + 2));
+          venn[IW] = dw - (c13 + c23 + (c123 + 2));
+          venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
+          for (int r = 0; r < p.rot.count; r++) acc += fc3(p.rot.fr[r], venn);
+        }
+      }
+      if (found) { i++; k++; }
+    }
+  }
+  block_sum_to(acc, slot);
+}
+
+// ------------------------------------------------------------- wedge core
+struct WedgeParams {
+  int f_v, f_vw, f_w;  // fringes of the larger-id endpoint, both, the other
+  int lim, minsum;     // min(min_v, min_w) and min_v + min_w
+};
+
+// Centre without fringes (wedgecore_specialized, src/fringeCount.cu:1409-1477).
+// One block per endpoint v (taken from a queue); for every centre u in N(v)
+// and every w < v in N(u) the pair (v, w) gets one more centre in a dense
+// per-block counter; then every touched pair is evaluated once with its
+// centre count C: C * wedge(v, w, C - 1).
+__global__ void __launch_bounds__(512) wedge_pair_kernel(GView g, WedgeParams p, unsigned* __restrict__ cnt_all,
+                                                         int* __restrict__ touched_all, int* __restrict__ queue,
+                                                         u64* __restrict__ slot) {
+  __shared__ int s_v, s_nt;
+  unsigned* cnt = cnt_all + (size_t)blockIdx.x * (size_t)g.n;
+  int* touched = touched_all + (size_t)blockIdx.x * (size_t)g.n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  u64 acc = 0;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_v = atomicAdd(queue, 1);
+      s_nt = 0;
+    }
+    __syncthreads();
+    const int v = s_v;
+    if (v >= g.n) break;
+    const int dv = g.deg[v];
+    if (dv >= p.lim) {
+      const int thres = max(p.lim, p.minsum - dv);
+      const long long vb = g.off[v];
+      for (int t = warp; t < dv; t += nwarp) {
+        const int u = g.adj[vb + t];
+        const long long ub = g.off[u];
+        const int du = g.deg[u];
+        for (int s = lane; s < du; s += 32) {
+          const int w = __ldg(g.adj + ub + s);
+          if (w >= v) break;
+          if (g.deg[w] >= thres) {
+            const unsigned old = atomicAdd(cnt + w, 1u);
+            if (old == 0) touched[atomicAdd(&s_nt, 1)] = w;
+          }
+        }
+      }
+      __syncthreads();
+      const int nt = s_nt;
+      const int* Nv = g.adj + vb;
+      for (int q = threadIdx.x; q < nt; q += blockDim.x) {
+        const int w = touched[q];
+        const unsigned C = cnt[w];
+        cnt[w] = 0;
+        const bool vw = bsearch_has(Nv, dv, w);
+        acc += (u64)C * wedge_formula(dv, g.deg[w], vw, p.f_v, p.f_vw, p.f_w, (int)C - 1);
+      }
+    }
+    __syncthreads();
+  }
+  block_sum_to(acc, slot);
+}
+
+struct GWedgeParams {
+  int min_u, lim, sum1, sum2, sum3;
+  Rot3 rot;
+};
+
+// Centre with fringes (general_wedge_core, src/fringeCount.cu:1480-1650): one
+// warp per centre u, looping over endpoints v in N(u); lanes take w in N(u),
+// w < v; open wedges use rotations 0 (and 3), triangles (counted once, with
+// u < w < v) use all rotations.
+__global__ void wedge_general_kernel(GView g, GWedgeParams p, u64* __restrict__ slot) {
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  u64 acc = 0;
+  for (int u = wid; u < g.n; u += nw) {
+    const int du = g.deg[u];
+    if (du < p.sum1) continue;
+    const long long ub = g.off[u];
+    const int* Nu = g.adj + ub;
+    const int th1u = max(p.sum1, p.sum2 - du);
+    for (int iv = 0; iv < du; iv++) {
+      const int v = __ldg(Nu + iv);
+      const int dv = g.deg[v];
+      if (dv < th1u) continue;  // init_wl_wedge
+      const int* Nv = g.adj + g.off[v];
+      // p12 = |N(u) & N(v)|
+      int p12 = 0;
+      {
+        const int* S = (du <= dv) ? Nu : Nv;
+        const int* L = (du <= dv) ? Nv : Nu;
+        const int ls = min(du, dv), ll = max(du, dv);
+        for (int t = lane; t < ls; t += 32) p12 += bsearch_has(L, ll, __ldg(S + t));
+        p12 = __reduce_add_sync(0xffffffffu, p12);
+      }
+      const bool cond = (du >= p.min_u) && (dv >= p.lim);
+      const int thres1 = max(p.lim, p.sum2 - dv);
+      const int thres2 = max(max(p.sum1, p.sum3 - du - dv), max(p.sum2 - du, p.sum2 - dv));
+      for (int t0 = 0; t0 < du; t0 += 32) {
+        const int t = t0 + lane;
+        bool active = false, tri = false;
+        int w = 0, dw = 0;
+        if (t < du) {
+          w = __ldg(Nu + t);
+          if (w < v) {
+            dw = g.deg[w];
+            if (dw >= thres2) {
+              tri = bsearch_has(Nv, dv, w);
+              active = tri ? (u < w) : (cond && dw >= thres1);
+            }
+          }
+        }
+        if (!__any_sync(0xffffffffu, t < du && w < v)) break;
+        unsigned bal = __ballot_sync(0xffffffffu, active);
+        int t13 = 0, t23 = 0, t123 = 0;
+        while (bal) {
+          const int who = __ffs(bal) - 1;
+          bal &= bal - 1;
+          const int ww = __shfl_sync(0xffffffffu, w, who);
+          const int dww = __shfl_sync(0xffffffffu, dw, who);
+          const int* Nw = g.adj + g.off[ww];
+          int a13 = 0, a23 = 0, a123 = 0;
+          for (int q = lane; q < dww; q += 32) {
+            const int x = __ldg(Nw + q);
+            const bool b13 = bsearch_has(Nu, du, x), b23 = bsearch_has(Nv, dv, x);
+            a13 += b13; a23 += b23; a123 += (b13 && b23);
+          }
+          a13 = __reduce_add_sync(0xffffffffu, a13);
+          a23 = __reduce_add_sync(0xffffffffu, a23);
+          a123 = __reduce_add_sync(0xffffffffu, a123);
+          if (lane == who) { t13 = a13; t23 = a23; t123 = a123; }
+        }
+        if (active) {
+          // common3_wedge (src/fringeCount.cu:1480-1510) + corrections
+          int venn[8];
+          const int c123 = t123, c12 = p12 - c123, c13 = t13 - c123, c23 = t23 - c123;
+          venn[0] = 0;
+          venn[IU] = du - (p12 + c13);
+          venn[IV] = dv - (p12 + c23);
+          venn[IW] = dw - (c13 + c23 + c123);
+          venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
+          if (tri) {
+            venn[IUV]--; venn[IUW]--; venn[IVW]--;
+            for (int r = 0; r < p.rot.count; r++) acc += fc3(p.rot.fr[r], venn);
+          } else {
+            venn[IU] -= 2; venn[IVW]--;
+            acc += fc3(p.rot.fr[0], venn);
+            if (p.rot.count > 3) acc += fc3(p.rot.fr[3], venn);
+          }
+        }
+      }
+    }
+  }
+  block_sum_to(acc, slot);
+}
+
+// ------------------------------------------------------------- general core
+constexpr int kMaxSlots = 665;  // 3^6 - 2^6: (anchor set, region) pairs for 6 anchors
+
+struct GenParams {
+  int k;           // core vertices
+  int anchors;     // bitmask of anchoring core vertices
+  int nonanchors;  // the other core vertices
+  int startdeg;
+  uint8_t destdeg[5];
+  uint8_t list[5];
+  int nslots;
+  uint8_t slot_idx[kMaxSlots];  // region bitmap of each placement step
+  uint8_t slot_set[kMaxSlots];  // anchor set index of each step
+  uint8_t slot_top[kMaxSlots];  // 1 if the step takes all remaining fringes
+  uint8_t fcnt[63];
+};
+
+// Placement sum (functionX, src/fringeCount.cu:408-486) over the precomputed
+// step list: step s puts a fringes of its anchor set into region slot_idx[s];
+// the last step of each set takes all its remaining fringes.  Each complete
+// placement adds the product of nck(remaining region size, fringes placed).
+__device__ u64 placement_sum(const GenParams& p, int* venn) {
+  int a_[kMaxSlots];
+  int rem_[kMaxSlots];
+  u64 pre_[kMaxSlots];
+  const int S = p.nslots;
+  u64 sum = 0;
+  int s = 0;
+  rem_[0] = p.fcnt[p.slot_set[0]];
+  pre_[0] = 1;
+  a_[0] = p.slot_top[0] ? rem_[0] : min(venn[p.slot_idx[0]], rem_[0]);
+  while (s >= 0) {
+    if (a_[s] < 0) {  // this step is exhausted: back up
+      s--;
+      if (s >= 0) {
+        venn[p.slot_idx[s]] += a_[s];
+        a_[s] = p.slot_top[s] ? -1 : a_[s] - 1;
+      }
+      continue;
+    }
+    const int idx = p.slot_idx[s];
+    const u64 w = pre_[s] * nck(venn[idx], a_[s]);
+    if (w == 0 || s == S - 1) {
+      sum += w;
+      a_[s] = p.slot_top[s] ? -1 : a_[s] - 1;
+      continue;
+    }
+    venn[idx] -= a_[s];
+    const int ns = s + 1;
+    pre_[ns] = w;
+    rem_[ns] = p.slot_top[s] ? (int)p.fcnt[p.slot_set[ns]] : rem_[s] - a_[s];
+    a_[ns] = p.slot_top[ns] ? rem_[ns] : min(venn[p.slot_idx[ns]], rem_[ns]);
+    s = ns;
+  }
+  return sum;
+}
+
+constexpr int kGenWarps = 4;  // warps per block in the general-core kernel
+
+struct GenWarp {
+  int stack[6];
+  int venn[32][64];  // one Venn row per lane (the lane that owns the match)
+};
+
+// exclusive Venn sizes of the current match into row[]; warp-cooperative
+__device__ void venn_general(const GView& g, const GenParams& p, const int* stack, int* row) {
+  const int lane = threadIdx.x & 31;
+  const int top = 1 << p.k;
+  for (int i = lane; i < 64; i += 32) row[i] = 0;
+  __syncwarp();
+  // each neighbour x of an anchor is counted once, from the lowest anchor it
+  // touches, under the exact set of anchors it touches
+  for (int i = 0; i < p.k; i++) {
+    if (!(p.anchors & (1 << i))) continue;
+    const int vi = stack[i];
+    const long long b = g.off[vi];
+    const int d = (int)(g.off[vi + 1] - b);
+    for (int t = lane; t < d; t += 32) {
+      const int x = __ldg(g.adj + b + t);
+      int bmp = 1 << i;
+      bool first = true;
+      for (int q = 0; q < p.k && first; q++) {
+        if (q == i || !(p.anchors & (1 << q))) continue;
+        const int vq = stack[q];
+        const long long qb = g.off[vq];
+        if (bsearch_has(g.adj + qb, (int)(g.off[vq + 1] - qb), x)) {
+          if (q < i) first = false;
+          else bmp |= 1 << q;
+        }
+      }
+      if (first) atomicAdd(row + bmp, 1);
+    }
+  }
+  __syncwarp();
+  // core vertices themselves are not fringe candidates
+  if (lane < p.k) {
+    const int x = stack[lane];
+    int bmp = 0;
+    for (int q = 0; q < p.k; q++) {
+      if (!(p.anchors & (1 << q))) continue;
+      const int vq = stack[q];
+      const long long qb = g.off[vq];
+      if (bsearch_has(g.adj + qb, (int)(g.off[vq + 1] - qb), x)) bmp |= 1 << q;
+    }
+    if (bmp) atomicSub(row + bmp, 1);
+  }
+  __syncwarp();
+  (void)top;
+}
+
+template <int L>
+__device__ u64 gen_level(const GView& g, const GenParams& p, GenWarp& w) {
+  // choose stack[L+1] among the neighbours of the first core vertex it must touch
+  const int lane = threadIdx.x & 31;
+  const int list = p.list[L];
+  const int first = __ffs(list) - 1;
+  const int src = w.stack[first];
+  const long long sb = g.off[src];
+  const int sd = (int)(g.off[src + 1] - sb);
+  const bool last = (L + 1 == p.k - 1);
+  u64 acc = 0;
+  for (int t0 = 0; t0 < sd; t0 += 32) {
+    const int t = t0 + lane;
+    bool ok = false;
+    int x = -1;
+    if (t < sd) {
+      x = __ldg(g.adj + sb + t);
+      ok = g.deg[x] >= p.destdeg[L];
+      for (int q = 0; q <= L && ok; q++) {
+        if (list & (1 << q)) {
+          if (q != first) {
+            const int vq = w.stack[q];
+            const long long qb = g.off[vq];
+            ok = bsearch_has(g.adj + qb, (int)(g.off[vq + 1] - qb), x);
+          }
+        } else {
+          ok = (w.stack[q] != x);
+        }
+      }
+    }
+    unsigned bal = __ballot_sync(0xffffffffu, ok);
+    if (last) {
+      unsigned rows = bal;
+      while (rows) {
+        const int who = __ffs(rows) - 1;
+        rows &= rows - 1;
+        const int xx = __shfl_sync(0xffffffffu, x, who);
+        if (lane == 0) w.stack[L + 1] = xx;
+        __syncwarp();
+        venn_general(g, p, w.stack, w.venn[who]);
+      }
+      __syncwarp();
+      if (ok) acc += placement_sum(p, w.venn[lane]);
+      __syncwarp();
+    } else {
+      while (bal) {
+        const int who = __ffs(bal) - 1;
+        bal &= bal - 1;
+        const int xx = __shfl_sync(0xffffffffu, x, who);
+        if (lane == 0) w.stack[L + 1] = xx;
+        __syncwarp();
+        if constexpr (L < 4) acc += gen_level<L + 1>(g, p, w);
+      }
+    }
+  }
+  return acc;
+}
+
+// one warp per directed edge (u, v): u = core vertex A, v = core vertex B
+__global__ void __launch_bounds__(kGenWarps * 32) general_core_kernel(GView g, const __grid_constant__ GenParams p,
+                                                                       int* __restrict__ queue, u64* __restrict__ slot) {
+  __shared__ GenWarp sw[kGenWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  GenWarp& w = sw[warp];
+  u64 acc = 0;
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(queue, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= g.n) break;
+    const int du = g.deg[u];
+    if (du < p.startdeg) continue;
+    const long long ub = g.off[u];
+    for (int iv = 0; iv < du; iv++) {
+      const int v = __ldg(g.adj + ub + iv);
+      if (g.deg[v] < p.destdeg[0]) continue;  // init_wl_general
+      if (lane == 0) { w.stack[0] = u; w.stack[1] = v; }
+      __syncwarp();
+      acc += gen_level<1>(g, p, w);
+      __syncwarp();
+    }
+  }
+  block_sum_to(acc, slot);
+}
+
+// ------------------------------------------------------------- host helpers
+void rotations3(const int f[8], bool wedge, Rot3& r) {
+  auto rot = [](const int* q, int* o) {
+    o[0] = 0; o[IUVW] = q[IUVW]; o[IUV] = q[IVW]; o[IUW] = q[IUV]; o[IVW] = q[IUW];
+    o[IU] = q[IV]; o[IV] = q[IW]; o[IW] = q[IU];
+  };
+  auto rot2 = [](const int* q, int* o) {
+    o[0] = 0; o[IUVW] = q[IUVW]; o[IUV] = q[IUW]; o[IUW] = q[IVW]; o[IVW] = q[IUV];
+    o[IU] = q[IW]; o[IV] = q[IU]; o[IW] = q[IV];
+  };
+  for (int i = 0; i < 8; i++) r.fr[0][i] = (i == 0) ? 0 : f[i];
+  r.count = 1;
+  // triangleRotations (src/fringeCount.cu:1291-1317) / wedgeRotations (:1754-1780)
+  const bool any = wedge || f[IU] != f[IV] || f[IU] != f[IW] || f[IUV] != f[IUW] || f[IUV] != f[IVW];
+  if (!any) return;
+  rot(r.fr[0], r.fr[1]);
+  rot2(r.fr[0], r.fr[2]);
+  r.count = 3;
+  const bool fl = wedge ? (f[IV] != f[IW] || f[IUV] != f[IUW])
+                        : ((f[IV] != f[IW] || f[IUV] != f[IUW]) && (f[IU] != f[IW] || f[IUV] != f[IVW]) &&
+                           (f[IU] != f[IV] || f[IUW] != f[IVW]));
+  if (!fl) return;
+  int* q = r.fr[3];
+  q[0] = 0; q[IUVW] = f[IUVW]; q[IUV] = f[IUW]; q[IUW] = f[IUV]; q[IVW] = f[IVW];
+  q[IU] = f[IU]; q[IV] = f[IW]; q[IW] = f[IV];
+  rot(r.fr[3], r.fr[4]);
+  rot2(r.fr[3], r.fr[5]);
+  r.count = 6;
+}
+
+int grid_for(long long work, int tpb, int per_sm) {
+  const long long want = (work + tpb - 1) / tpb;
+  const long long cap = (long long)sm_count() * per_sm;
+  return (int)std::max(1LL, std::min(want, cap));
+}
+
+// Pair-counter scratch for the wedge core: `blocks` rows of n counters plus
+// `blocks` rows of n touched-list entries.  Counters are zero whenever no
+// kernel is running (each launch clears what it touched), so they are only
+// cleared when the row layout changes.
+int ensure_pair_scratch(Scratch& sc, int n, int blocks, cudaStream_t s) {
+  const size_t need = (size_t)blocks * (size_t)n * (sizeof(unsigned) + sizeof(int));
+  if (sc.bytes < need) {
+    if (sc.ptr) {
+      cudaStreamSynchronize(s);
+      cudaFree(sc.ptr);
+      sc.ptr = nullptr;
+      sc.bytes = 0;
+    }
+    if (cudaMalloc(&sc.ptr, need) != cudaSuccess) {
+      cudaGetLastError();
+      return FSGC_ENOMEM;
+    }
+    sc.bytes = need;
+    sc.layout_n = -1;
+  }
+  if (sc.layout_n != n || sc.layout_rows != blocks) {
+    if (cudaMemsetAsync(sc.ptr, 0, (size_t)blocks * (size_t)n * sizeof(unsigned), s) != cudaSuccess) return FSGC_ECUDA;
+    sc.layout_n = n;
+    sc.layout_rows = blocks;
+  }
+  return FSGC_OK;
+}
+
+}  // namespace
+
+int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work) {
+  const fsgc_matching_order& mo = *job.mo;
+  DevGraph& G = *job.g;
+  job.host_only = false;
+  job.host_value = 0;
+  if (mo.nodes < 1 || mo.nodes > FSGC_MAX_CORE || mo.anchorsets > 63) return FSGC_EINVAL;
+  const int TPB = kTPB;
+
+  // ---- vertex core (vertexCore, src/fringeCount.cu:2172-2191)
+  if (mo.nodes == 1) {
+    job.core_type = FSGC_CORE_VERTEX;
+    if (mo.anchorsets == 0) { job.host_only = true; job.host_value = (u64)G.n; return FSGC_OK; }
+    if (mo.fcnt[0] == 1) { job.host_only = true; job.host_value = (u64)(G.m / 2); return FSGC_OK; }
+    star_kernel<<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(G.view(), mo.fcnt[0], job.d_slot);
+    *launches += 1;
+    return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+  }
+
+  int st = prepare_graph(G, s, launches, work.small);
+  if (st != FSGC_OK) return st;
+  GView gv = G.view();
+  const long long me = G.m / 2;
+
+  // ---- edge core (edgeCore, src/fringeCount.cu:2106-2144)
+  if (mo.nodes == 2) {
+    job.core_type = FSGC_CORE_EDGE;
+    int f[4] = {0, 0, 0, 0};
+    for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 3] = mo.fcnt[i];
+    const int f_u = std::min(f[1], f[2]), f_uv = f[3], f_v = std::max(f[1], f[2]);
+    if (f_uv == 1 && (f_u == 0 || f_v == 0)) {
+      if (f_u == 0 && f_v == 0) {  // triangle
+        job.host_only = true;
+        job.host_value = (u64)G.triangles;
+        return FSGC_OK;
+      }
+      st = ensure_vertex_triangles(G, s, launches);
+      if (st != FSGC_OK) return st;
+      tailed_triangle_kernel<<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(gv, G.vtri2, f_v, job.d_slot);
+      *launches += 1;
+      return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+    }
+    EdgeParams ep{f_u, f_uv, f_v, f_u + f_uv, f_u + f_uv + f_v};
+    if (me > 0) {
+      edge_kernel<<<grid_for(me, TPB, 8), TPB, 0, s>>>(gv, ep, job.d_slot);
+      *launches += 1;
+    }
+    return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+  }
+
+  int f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (mo.nodes == 3)
+    for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 7] = mo.fcnt[i];
+
+  // ---- wedge core (wedgeCore, src/fringeCount.cu:1783-1825)
+  if (mo.nodes == 3 && __builtin_popcount(mo.list[1]) == 1) {
+    job.core_type = FSGC_CORE_WEDGE;
+    if (mo.list[1] == 2) {  // centre is B: swap roles of A and B
+      std::swap(f[IU], f[IV]);
+      std::swap(f[IUW], f[IVW]);
+    }
+    const int min_u = f[IUVW] + f[IUV] + f[IUW] + f[IU] + 2;
+    const int min_v = f[IUVW] + f[IUV] + f[IVW] + f[IV] + 1;
+    const int min_w = f[IUVW] + f[IUW] + f[IVW] + f[IW] + 1;
+    const int sum3 = min_u + min_v + min_w;
+    const int sum2 = sum3 - std::max(std::max(min_u, min_v), min_w);
+    const int sum1 = std::min(std::min(min_u, min_v), min_w);
+    const int lim = std::min(min_v, min_w);
+    if (f[IUVW] == 0 && f[IUV] == 0 && f[IUW] == 0 && f[IU] == 0) {
+      WedgeParams wp{f[IV], f[IVW], f[IW], lim, min_v + min_w};
+      // dense per-block pair counters + touched lists, bounded to 16 GiB
+      const size_t per_block = (size_t)G.n * (sizeof(unsigned) + sizeof(int));
+      int blocks = sm_count() * 2;
+      const size_t budget = (size_t)16 << 30;
+      blocks = (int)std::max<size_t>(1, std::min<size_t>((size_t)blocks, budget / std::max<size_t>(1, per_block)));
+      st = ensure_pair_scratch(work.pairs, G.n, blocks, s);
+      if (st != FSGC_OK) return st;
+      int* queue = reinterpret_cast<int*>(work.small + 4);
+      cudaMemsetAsync(queue, 0, sizeof(int), s);
+      unsigned* cnt = reinterpret_cast<unsigned*>(work.pairs.ptr);
+      int* touched = reinterpret_cast<int*>(cnt + (size_t)blocks * G.n);
+      wedge_pair_kernel<<<blocks, 512, 0, s>>>(gv, wp, cnt, touched, queue, job.d_slot);
+      *launches += 1;
+      return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+    }
+    GWedgeParams gp;
+    gp.min_u = min_u; gp.lim = lim; gp.sum1 = sum1; gp.sum2 = sum2; gp.sum3 = sum3;
+    rotations3(f, true, gp.rot);
+    wedge_general_kernel<<<grid_for((long long)G.n * 32, TPB, 8), TPB, 0, s>>>(gv, gp, job.d_slot);
+    *launches += 1;
+    return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+  }
+
+  // ---- triangle core (triangleCore, src/fringeCount.cu:1320-1373)
+  if (mo.nodes == 3) {
+    job.core_type = FSGC_CORE_TRIANGLE;
+    const int min_u = f[IUVW] + f[IUV] + f[IUW] + f[IU];
+    const int min_v = f[IUVW] + f[IUV] + f[IVW] + f[IV];
+    const int min_w = f[IUVW] + f[IUW] + f[IVW] + f[IW];
+    TriParams tp;
+    tp.sum3 = min_u + min_v + min_w + 6;
+    tp.sum2 = tp.sum3 - (std::max(std::max(min_u, min_v), min_w) + 2);
+    tp.sum1 = std::min(std::min(min_u, min_v), min_w) + 2;
+    const bool clique = (f[IUVW] == 1) && (f[IUV] + f[IUW] + f[IVW] == 0) &&
+                        ((f[IU] == 0) + (f[IV] == 0) + (f[IW] == 0) >= 2);
+    tp.tails = f[IU] + f[IV] + f[IW];
+    tp.mode = clique ? (tp.tails == 0 ? 1 : 2) : 0;
+    tp.relabel = G.tri_relabel ? 1 : 0;
+    rotations3(f, false, tp.rot);
+    if (me > 0) {
+      triangle_core_kernel<<<grid_for(me, TPB, 8), TPB, 0, s>>>(gv, tp, job.d_slot);
+      *launches += 1;
+    }
+    return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+  }
+
+  // ---- general core (generalCore, src/fringeCount.cu:666-692)
+  job.core_type = FSGC_CORE_GENERAL;
+  if (mo.anchorsets == 0) return FSGC_EINVAL;
+  GenParams* gp = new GenParams();
+  memset(gp, 0, sizeof(GenParams));
+  gp->k = mo.nodes;
+  for (int i = 0; i < mo.anchorsets; i++) gp->anchors |= mo.anch[i];
+  gp->nonanchors = gp->anchors ^ ((1 << mo.nodes) - 1);
+  gp->startdeg = mo.startdeg;
+  for (int i = 0; i < 5; i++) { gp->destdeg[i] = mo.destdeg[i]; gp->list[i] = mo.list[i]; }
+  for (int i = 0; i < 63; i++) gp->fcnt[i] = mo.fcnt[i];
+  // placement steps: anchor sets from the last to the first; within a set the
+  // regions containing it in increasing bitmap order, the all-anchor region last
+  int ns = 0;
+  for (int asi = mo.anchorsets - 1; asi >= 0; asi--) {
+    const int anch = mo.anch[asi];
+    int idx = anch;
+    for (;;) {
+      if (ns >= kMaxSlots) { delete gp; return FSGC_EUNSUPPORTED; }
+      gp->slot_idx[ns] = (uint8_t)idx;
+      gp->slot_set[ns] = (uint8_t)asi;
+      gp->slot_top[ns] = (idx == gp->anchors) ? 1 : 0;
+      ns++;
+      if (idx == gp->anchors) break;
+      idx = (((idx | gp->nonanchors) + 1) | anch) & ~gp->nonanchors;
+    }
+  }
+  gp->nslots = ns;
+  int* queue = reinterpret_cast<int*>(work.small + 5);
+  cudaMemsetAsync(queue, 0, sizeof(int), s);
+  const int blocks = sm_count() * 8;
+  general_core_kernel<<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
+  *launches += 1;
+  delete gp;
+  return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+
+}  // namespace fsgc

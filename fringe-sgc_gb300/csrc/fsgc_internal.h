@@ -1,0 +1,93 @@
+// Internal types shared by the library's translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fsgc.h"
+#include "fsgc_device.cuh"
+
+namespace fsgc {
+
+// Graph resident in HBM.  Full CSR (int64 offsets, int32 sorted lists) plus the
+// loader's derived structures:
+//  - degree order:  x < y  iff  (deg x, x) < (deg y, y); every undirected edge
+//    is stored once, from its lower to its higher endpoint ("oriented" CSR);
+//  - osrc: the lower endpoint of each oriented slot (edge-parallel kernels);
+//  - osup: per oriented slot, |N(x) & N(y)| (triangles through the edge);
+//  - vtri2: per vertex, twice its triangle count (lazily).
+struct GView {
+  int n;
+  long long m;                       // directed entries
+  const long long* __restrict__ off;  // n+1
+  const int* __restrict__ adj;        // m
+  const int* __restrict__ deg;        // n
+  const long long* __restrict__ ooff; // n+1
+  const int* __restrict__ oadj;       // m/2
+  const int* __restrict__ osrc;       // m/2
+  const unsigned* __restrict__ osup;  // m/2
+};
+
+struct DevGraph {
+  int n = 0;
+  long long m = 0;
+  long long* off = nullptr;
+  int* adj = nullptr;
+  int* deg = nullptr;
+  int maxdeg = 0;
+  // orientation + supports (built by prepare_graph)
+  bool prepared = false;
+  long long* ooff = nullptr;
+  int* oadj = nullptr;
+  int* osrc = nullptr;
+  unsigned* osup = nullptr;
+  long long triangles = -1;
+  u64* vtri2 = nullptr;  // lazily
+  // the reference's degree-relabel gate for the triangle core
+  // (src/fringeCount.cu:1237, 1342-1344): vertex roles follow (deg, id) order
+  // when it fires, vertex ids otherwise
+  bool tri_relabel = false;
+  size_t bytes = 0;
+
+  GView view() const {
+    GView g;
+    g.n = n; g.m = m; g.off = off; g.adj = adj; g.deg = deg;
+    g.ooff = ooff; g.oadj = oadj; g.osrc = osrc; g.osup = osup;
+    return g;
+  }
+};
+
+// Device scratch arena owned by a context; grows on demand, never shrinks.
+struct Scratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int layout_n = -1, layout_rows = -1;
+};
+
+// Per-context device work areas: a few u64 counters/queues and the wedge-core
+// pair counters.
+struct DevWork {
+  u64* small = nullptr;  // 32 u64
+  Scratch pairs;
+};
+
+struct Launcher;  // forward
+
+// Entry points implemented in prep.cu / count.cu.
+int prepare_graph(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_scratch_u64);
+int ensure_vertex_triangles(DevGraph& g, cudaStream_t s, uint64_t* launches);
+void upload_div_magic();
+int sm_count();
+
+struct CountJob {
+  const fsgc_matching_order* mo;
+  DevGraph* g;
+  u64* d_slot;        // result slot (zeroed by the caller)
+  int core_type;      // out
+  u64 host_value;     // used when the result needs no device work (n, m/2, T)
+  bool host_only;
+};
+
+// Enqueue the kernels that add the raw total of `mo` on `g` into *d_slot.
+int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work);
+
+}  // namespace fsgc

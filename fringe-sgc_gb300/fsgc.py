@@ -1,0 +1,286 @@
+"""ctypes binding of libfsgc (include/fsgc.h) for tests, benchmarks and scripts.
+
+The binding only marshals arguments; all counting happens in the CUDA library.
+Loading fails loudly when libfsgc.so has not been built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfsgc.so")
+
+MO_SIZE = 139
+CORE_NAMES = {1: "vertex", 2: "edge", 3: "wedge", 4: "triangle", 5: "general"}
+
+
+class MatchingOrder(C.Structure):
+    _pack_ = 1
+    _fields_ = [("nodes", C.c_uint8), ("anchorsets", C.c_uint8), ("startdeg", C.c_uint8),
+                ("destdeg", C.c_uint8 * 5), ("list", C.c_uint8 * 5), ("anch", C.c_uint8 * 63),
+                ("fcnt", C.c_uint8 * 63)]
+
+    def to_bytes(self):
+        return bytes(C.string_at(C.addressof(self), MO_SIZE))
+
+    @classmethod
+    def from_bytes(cls, b):
+        assert len(b) == MO_SIZE
+        mo = cls()
+        C.memmove(C.addressof(mo), b, MO_SIZE)
+        return mo
+
+
+assert C.sizeof(MatchingOrder) == MO_SIZE
+
+
+class Result(C.Structure):
+    _fields_ = [("count", C.c_uint64), ("raw_total", C.c_uint64), ("automorphisms", C.c_uint64),
+                ("flags", C.c_uint32), ("core_type", C.c_int32), ("device_ms", C.c_double)]
+
+
+class Task(C.Structure):
+    _pack_ = 1
+    _fields_ = [("gid", C.c_int32), ("mo", MatchingOrder)]
+
+
+class HostCSR(C.Structure):
+    _fields_ = [("n", C.c_int32), ("m", C.c_int64), ("nindex", C.POINTER(C.c_int64)),
+                ("nlist", C.POINTER(C.c_int32))]
+
+
+class GraphInfo(C.Structure):
+    _fields_ = [("n", C.c_int32), ("m", C.c_int64), ("max_degree", C.c_int32), ("triangles", C.c_int64),
+                ("device_bytes", C.c_int64)]
+
+
+class FsgcError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FsgcError(f"libfsgc.so not built at {LIB_PATH}; run fringe-sgc_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        P, I, I64, U64 = C.c_void_p, C.c_int, C.c_int64, C.c_uint64
+        sig = {
+            "fsgc_preprocess": (I, [I, C.POINTER(C.c_int), I, C.POINTER(MatchingOrder), C.c_char_p, I]),
+            "fsgc_preprocess_predefined": (I, [I, C.POINTER(MatchingOrder), C.c_char_p, I]),
+            "fsgc_predefined_pattern": (I, [I, C.POINTER(C.c_int), C.POINTER(C.c_int), I, C.POINTER(C.c_int)]),
+            "fsgc_predefined_name": (C.c_char_p, [I]),
+            "fsgc_egr_read": (I, [C.c_char_p, C.POINTER(HostCSR)]),
+            "fsgc_egr_write": (I, [C.c_char_p, C.POINTER(HostCSR)]),
+            "fsgc_csr_validate": (I, [C.POINTER(HostCSR), C.c_char_p, I]),
+            "fsgc_gen_rmat": (I, [I, I, C.c_double, C.c_double, C.c_double, U64, C.POINTER(HostCSR)]),
+            "fsgc_gen_er": (I, [I, I64, U64, C.POINTER(HostCSR)]),
+            "fsgc_gen_chung_lu": (I, [I, C.c_double, C.c_double, U64, C.POINTER(HostCSR)]),
+            "fsgc_csr_from_edges": (I, [I, I64, C.POINTER(C.c_int32), C.POINTER(HostCSR)]),
+            "fsgc_host_csr_pin": (I, [C.POINTER(HostCSR)]),
+            "fsgc_host_csr_free": (None, [C.POINTER(HostCSR)]),
+            "fsgc_ctx_create": (I, [I, C.POINTER(P)]),
+            "fsgc_ctx_destroy": (None, [P]),
+            "fsgc_ctx_last_error": (C.c_char_p, [P]),
+            "fsgc_ctx_stream": (P, [P]),
+            "fsgc_ctx_launches": (U64, [P]),
+            "fsgc_graph_from_csr": (I, [P, I, I64, P, P, C.POINTER(C.c_int)]),
+            "fsgc_graph_from_csr32": (I, [P, I, I, P, P, C.POINTER(C.c_int)]),
+            "fsgc_graph_from_device_csr": (I, [P, I, I64, P, P, C.POINTER(C.c_int)]),
+            "fsgc_graph_load_egr": (I, [P, C.c_char_p, C.POINTER(C.c_int)]),
+            "fsgc_graph_release": (I, [P, I]),
+            "fsgc_graph_info_get": (I, [P, I, C.POINTER(GraphInfo)]),
+            "fsgc_count": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(Result)]),
+            "fsgc_count_batch": (I, [P, C.POINTER(Task), I, C.POINTER(Result)]),
+            "fsgc_nck_host": (C.c_ulonglong, [I, I]),
+            "fsgc_div_small_host": (C.c_ulonglong, [C.c_ulonglong, C.c_uint]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(st, what, ctx=None):
+    if st != 0:
+        msg = ""
+        if ctx is not None:
+            msg = lib().fsgc_ctx_last_error(ctx).decode(errors="replace")
+        raise FsgcError(f"{what} failed with status {st}: {msg}")
+
+
+# ----------------------------------------------------------------- patterns
+def preprocess(n, edges):
+    """Decompose a pattern (n vertices, list of (s, d) edges) into a MatchingOrder."""
+    flat = (C.c_int * (2 * len(edges) or 1))(*[int(x) for e in edges for x in e])
+    mo = MatchingOrder()
+    err = C.create_string_buffer(256)
+    st = lib().fsgc_preprocess(int(n), flat, len(edges), C.byref(mo), err, 256)
+    if st != 0:
+        raise FsgcError(f"preprocess: {err.value.decode()} (status {st})")
+    return mo
+
+
+def preprocess_predefined(number):
+    mo = MatchingOrder()
+    err = C.create_string_buffer(256)
+    st = lib().fsgc_preprocess_predefined(int(number), C.byref(mo), err, 256)
+    if st != 0:
+        raise FsgcError(f"preprocess_predefined: {err.value.decode()} (status {st})")
+    return mo
+
+
+def predefined_pattern(number):
+    n, ne = C.c_int(), C.c_int()
+    _check(lib().fsgc_predefined_pattern(number, C.byref(n), None, 0, C.byref(ne)), "predefined_pattern")
+    buf = (C.c_int * (2 * ne.value))()
+    _check(lib().fsgc_predefined_pattern(number, C.byref(n), buf, ne.value, C.byref(ne)), "predefined_pattern")
+    return n.value, [(buf[2 * i], buf[2 * i + 1]) for i in range(ne.value)]
+
+
+# ----------------------------------------------------------------- host graphs
+class Graph:
+    """Host CSR as numpy arrays: nindex int64[n+1], nlist int32[m]."""
+
+    def __init__(self, nindex, nlist):
+        self.nindex = np.ascontiguousarray(nindex, dtype=np.int64)
+        self.nlist = np.ascontiguousarray(nlist, dtype=np.int32)
+        self.n = len(self.nindex) - 1
+        self.m = int(self.nindex[-1])
+
+    def degrees(self):
+        return np.diff(self.nindex)
+
+    def as_host_csr(self):
+        h = HostCSR()
+        h.n = self.n
+        h.m = self.m
+        h.nindex = self.nindex.ctypes.data_as(C.POINTER(C.c_int64))
+        h.nlist = self.nlist.ctypes.data_as(C.POINTER(C.c_int32))
+        return h
+
+
+def _take(h):
+    n, m = h.n, h.m
+    idx = np.ctypeslib.as_array(h.nindex, shape=(n + 1,)).copy()
+    adj = np.ctypeslib.as_array(h.nlist, shape=(max(m, 1),))[:m].copy() if m > 0 else np.zeros(0, np.int32)
+    lib().fsgc_host_csr_free(C.byref(h))
+    return Graph(idx, adj)
+
+
+def gen_rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1):
+    h = HostCSR()
+    _check(lib().fsgc_gen_rmat(scale, edge_factor, a, b, c, seed, C.byref(h)), "gen_rmat")
+    return _take(h)
+
+
+def gen_er(n, m, seed=1):
+    h = HostCSR()
+    _check(lib().fsgc_gen_er(n, m, seed, C.byref(h)), "gen_er")
+    return _take(h)
+
+
+def gen_chung_lu(n, avg_degree, exponent, seed=1):
+    h = HostCSR()
+    _check(lib().fsgc_gen_chung_lu(n, avg_degree, exponent, seed, C.byref(h)), "gen_chung_lu")
+    return _take(h)
+
+
+def csr_from_edges(n, pairs):
+    arr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+    h = HostCSR()
+    _check(lib().fsgc_csr_from_edges(n, len(arr), arr.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(h)),
+           "csr_from_edges")
+    return _take(h)
+
+
+def egr_read(path):
+    h = HostCSR()
+    _check(lib().fsgc_egr_read(path.encode(), C.byref(h)), "egr_read")
+    return _take(h)
+
+
+def egr_write(path, g):
+    h = g.as_host_csr()
+    _check(lib().fsgc_egr_write(path.encode(), C.byref(h)), "egr_write")
+
+
+def validate(g):
+    h = g.as_host_csr()
+    err = C.create_string_buffer(256)
+    st = lib().fsgc_csr_validate(C.byref(h), err, 256)
+    return st, err.value.decode()
+
+
+# ----------------------------------------------------------------- device
+class Context:
+    def __init__(self, device=0):
+        self.ptr = C.c_void_p()
+        st = lib().fsgc_ctx_create(device, C.byref(self.ptr))
+        if st != 0:
+            raise FsgcError(f"fsgc_ctx_create failed with status {st} (no usable GB300 device or kernels)")
+
+    def close(self):
+        if self.ptr:
+            lib().fsgc_ctx_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def launches(self):
+        return int(lib().fsgc_ctx_launches(self.ptr))
+
+    @property
+    def stream(self):
+        return lib().fsgc_ctx_stream(self.ptr)
+
+    def upload(self, g):
+        gid = C.c_int()
+        _check(lib().fsgc_graph_from_csr(self.ptr, g.n, g.m, g.nindex.ctypes.data, g.nlist.ctypes.data,
+                                         C.byref(gid)), "graph_from_csr", self.ptr)
+        return gid.value
+
+    def upload_device(self, n, m, d_nindex, d_nlist):
+        gid = C.c_int()
+        _check(lib().fsgc_graph_from_device_csr(self.ptr, n, m, d_nindex, d_nlist, C.byref(gid)),
+               "graph_from_device_csr", self.ptr)
+        return gid.value
+
+    def load_egr(self, path):
+        gid = C.c_int()
+        _check(lib().fsgc_graph_load_egr(self.ptr, path.encode(), C.byref(gid)), "graph_load_egr", self.ptr)
+        return gid.value
+
+    def release(self, gid):
+        _check(lib().fsgc_graph_release(self.ptr, gid), "graph_release", self.ptr)
+
+    def info(self, gid):
+        gi = GraphInfo()
+        _check(lib().fsgc_graph_info_get(self.ptr, gid, C.byref(gi)), "graph_info", self.ptr)
+        return gi
+
+    def count(self, gid, mo):
+        r = Result()
+        _check(lib().fsgc_count(self.ptr, gid, C.byref(mo), C.byref(r)), "count", self.ptr)
+        return r
+
+    def count_batch(self, tasks):
+        """tasks: list of (gid, MatchingOrder)."""
+        arr = (Task * len(tasks))()
+        for i, (gid, mo) in enumerate(tasks):
+            arr[i].gid = gid
+            arr[i].mo = mo
+        res = (Result * len(tasks))()
+        _check(lib().fsgc_count_batch(self.ptr, arr, len(tasks), res), "count_batch", self.ptr)
+        return list(res)

@@ -1,0 +1,162 @@
+/*
+ * fsgc.h -- C ABI of the GB300-native fringe subgraph counter (libfsgc.so).
+ *
+ * The reference (Fringe-SGC) has no library interface: its boundary is two
+ * command-line programs and two binary formats.  Each entry point below names
+ * the reference code it stands in for.  Conventions:
+ *   - every call returns an fsgc_status (0 = success); nothing calls exit() or
+ *     traps on the device; fsgc_ctx_last_error() has the message;
+ *   - callers own host buffers, a context owns device memory;
+ *   - a context serialises its own calls with an internal lock, and any number
+ *     of contexts may live in one process.
+ */
+#ifndef FSGC_H
+#define FSGC_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSGC_MAX_CORE 6     /* src/fringes.h:44 */
+#define FSGC_MAX_PATTERN 32 /* src/patterns.h:45 */
+
+typedef enum fsgc_status {
+  FSGC_OK = 0,
+  FSGC_EINVAL = 1,       /* bad argument or malformed input */
+  FSGC_ENOMEM = 2,       /* device or host allocation failed */
+  FSGC_ECUDA = 3,        /* CUDA runtime error */
+  FSGC_EIO = 4,          /* file could not be read or written */
+  FSGC_EUNSUPPORTED = 5, /* e.g. a core of more than six vertices */
+  FSGC_ETIMEDOUT = 6,    /* a bounded device wait gave up */
+  FSGC_ENOTFOUND = 7,    /* unknown graph id or ticket */
+  FSGC_EBUSY = 8,        /* result not ready / admission refused */
+  FSGC_ENODEV = 9        /* no usable CUDA device or kernels not loaded */
+} fsgc_status;
+
+/* Matching order: byte-for-byte the reference's MatchingOrder
+ * (src/fringes.h:50-58), 139 packed bytes, the content of a `.mo` file. */
+typedef struct fsgc_matching_order {
+  uint8_t nodes;      /* core vertices (1..6) */
+  uint8_t anchorsets; /* number of distinct anchor sets */
+  uint8_t startdeg;   /* pattern degree of core vertex A */
+  uint8_t destdeg[FSGC_MAX_CORE - 1];
+  uint8_t list[FSGC_MAX_CORE - 1];               /* earlier core vertices each must touch */
+  uint8_t anch[(1 << FSGC_MAX_CORE) - 1];        /* anchor-set bitmaps */
+  uint8_t fcnt[(1 << FSGC_MAX_CORE) - 1];        /* fringes per anchor set */
+} fsgc_matching_order;
+
+typedef enum fsgc_core_type {
+  FSGC_CORE_VERTEX = 1,   /* vertexCore, src/fringeCount.cu:2172 */
+  FSGC_CORE_EDGE = 2,     /* edgeCore, :2106 */
+  FSGC_CORE_WEDGE = 3,    /* wedgeCore, :1783 */
+  FSGC_CORE_TRIANGLE = 4, /* triangleCore, :1320 */
+  FSGC_CORE_GENERAL = 5   /* generalCore, :666 */
+} fsgc_core_type;
+
+/* fsgc_result.flags */
+#define FSGC_FLAG_PATTERN_TOO_LARGE 0x1u /* pattern has more vertices/edges than the graph: count 0 */
+
+typedef struct fsgc_result {
+  uint64_t count;         /* the reference's printed count, as u64: raw_total / automorphisms */
+  uint64_t raw_total;     /* u64 total of the per-match formulas (the reference's `total`) */
+  uint64_t automorphisms; /* divisor: the pattern counted in itself (1 for vertex and edge cores) */
+  uint32_t flags;
+  int32_t core_type;      /* fsgc_core_type */
+  double device_ms;       /* device time of this count (CUDA events on the context stream) */
+} fsgc_result;
+
+typedef struct fsgc_ctx fsgc_ctx;
+
+/* ---- pattern decomposition (replaces fringePreprocess, src/fringePreprocess.cpp:287-365) ---- */
+
+/* n pattern vertices (2..32), nedges undirected edges as pairs in `edges`.
+ * Fills *out with the same matching order the reference CLI writes to motif.mo
+ * (bytes the reference leaves unwritten are zero). */
+int fsgc_preprocess(int n, const int* edges, int nedges, fsgc_matching_order* out, char* errbuf, int errlen);
+/* `fringePreprocess <motif_number>`: predefined motif 0..30 (src/patterns.h:57-354). */
+int fsgc_preprocess_predefined(int number, fsgc_matching_order* out, char* errbuf, int errlen);
+/* Same as fsgc_preprocess, writing the reference CLI's progress lines to `log`. */
+int fsgc_preprocess_log(int n, const int* edges, int nedges, fsgc_matching_order* out, char* errbuf, int errlen,
+                        FILE* log);
+/* Predefined motif as an edge list (edges may be NULL to query the size). */
+int fsgc_predefined_pattern(int number, int* n, int* edges, int max_edges, int* nedges);
+const char* fsgc_predefined_name(int number);
+
+/* ---- host-side graphs, ECLgraph files, generators (src/ECLgraph.h:45-96) ---- */
+
+/* Host CSR with 64-bit offsets: nindex[n+1], nlist[m] (m directed entries). */
+typedef struct fsgc_host_csr {
+  int32_t n;
+  int64_t m;
+  int64_t* nindex;
+  int32_t* nlist;
+} fsgc_host_csr;
+
+/* readECLgraph (src/ECLgraph.h:58-85): int32 header and arrays; weights ignored. */
+int fsgc_egr_read(const char* path, fsgc_host_csr* out);
+/* Writes the same format (int32 offsets; fails with FSGC_EUNSUPPORTED if m >= 2^31). */
+int fsgc_egr_write(const char* path, const fsgc_host_csr* g);
+/* Checks the reference's documented preconditions (src/fringeCount.cu:50-56):
+ * sorted, duplicate-free, loop-free, symmetric lists. */
+int fsgc_csr_validate(const fsgc_host_csr* g, char* errbuf, int errlen);
+/* Seeded synthetic graphs, symmetrised, deduplicated, self loops dropped. */
+int fsgc_gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, fsgc_host_csr* out);
+int fsgc_gen_er(int n, int64_t undirected_edges, uint64_t seed, fsgc_host_csr* out);
+int fsgc_gen_chung_lu(int n, double avg_degree, double exponent, uint64_t seed, fsgc_host_csr* out);
+/* Builds a cleaned CSR from an arbitrary undirected edge list (pairs). */
+int fsgc_csr_from_edges(int n, int64_t nedges, const int32_t* pairs, fsgc_host_csr* out);
+/* Page-locks a host CSR for fast uploads (optional). */
+int fsgc_host_csr_pin(fsgc_host_csr* g);
+void fsgc_host_csr_free(fsgc_host_csr* g);
+
+/* ---- contexts ---- */
+
+int fsgc_ctx_create(int device, fsgc_ctx** out);
+void fsgc_ctx_destroy(fsgc_ctx* ctx);
+const char* fsgc_ctx_last_error(const fsgc_ctx* ctx);
+/* The cudaStream_t on which the context runs all of its work. */
+void* fsgc_ctx_stream(fsgc_ctx* ctx);
+/* Number of this library's kernels launched by the context so far. */
+uint64_t fsgc_ctx_launches(const fsgc_ctx* ctx);
+
+/* ---- resident graphs (CSR upload + loader: src/fringeCount.cu:2286-2297) ---- */
+
+/* Uploads a host CSR (offsets 64-bit) and prepares it for counting. */
+int fsgc_graph_from_csr(fsgc_ctx* ctx, int n, int64_t m, const int64_t* nindex, const int32_t* nlist, int* gid);
+/* Same with the reference's int32 offsets (ECLgraph layout). */
+int fsgc_graph_from_csr32(fsgc_ctx* ctx, int n, int m, const int32_t* nindex, const int32_t* nlist, int* gid);
+/* Device-resident input (context's device): the arrays are copied, not adopted. */
+int fsgc_graph_from_device_csr(fsgc_ctx* ctx, int n, int64_t m, const int64_t* d_nindex, const int32_t* d_nlist,
+                               int* gid);
+int fsgc_graph_load_egr(fsgc_ctx* ctx, const char* path, int* gid);
+int fsgc_graph_release(fsgc_ctx* ctx, int gid);
+
+typedef struct fsgc_graph_info {
+  int32_t n;
+  int64_t m;            /* directed CSR entries */
+  int32_t max_degree;
+  int64_t triangles;    /* -1 until the triangle pass has run */
+  int64_t device_bytes; /* HBM held by this graph */
+} fsgc_graph_info;
+int fsgc_graph_info_get(fsgc_ctx* ctx, int gid, fsgc_graph_info* out);
+
+/* ---- counting (replaces `fringeCount <graph> <motif.mo>`, src/fringeCount.cu:2265-2331,
+ *      and occurrences(), :2199-2262) ---- */
+
+int fsgc_count(fsgc_ctx* ctx, int gid, const fsgc_matching_order* mo, fsgc_result* out);
+
+/* Many (graph, pattern) tasks in one call; results in task order. */
+typedef struct fsgc_task {
+  int32_t gid;
+  fsgc_matching_order mo;
+} fsgc_task;
+int fsgc_count_batch(fsgc_ctx* ctx, const fsgc_task* tasks, int ntasks, fsgc_result* results);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSGC_H */

@@ -1,0 +1,784 @@
+// fsgc oracle -- TEST INFRASTRUCTURE ONLY.
+//
+// A CPU restatement of Fringe-SGC's counting path (src/fringeCount.cu of the
+// reference) and an independent brute-force subgraph enumerator.  Only the test
+// suite, the smoke check and the CPU-baseline legs of bench.py load this
+// library; the product (libfsgc) never links, loads or calls it.
+//
+// Parity status: the restatement is pinned against the brute-force enumerator
+// and closed-form counts on graphs where the reference's u64 binomials do not
+// wrap.  The pattern decomposition is pinned byte-for-byte against the
+// reference's own fringePreprocess (built from its sources by oracle/Makefile).
+//
+// Every routine follows the reference one match at a time, with the same vertex
+// roles, the same pruning thresholds and the same binomial factorisation, so the
+// u64 totals agree bit for bit even where the reference's nCk wraps.  Summation
+// order is free: the reference only ever adds and multiplies mod 2^64 after nCk.
+//
+// Graph input: n vertices, int64 offsets idx[n+1], int32 sorted neighbour lists
+// adj[idx[n]] (symmetric, no self loops, no duplicates -- the reference's
+// documented preconditions, src/fringeCount.cu:50-56).
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <omp.h>
+
+typedef unsigned long long u64;
+typedef unsigned __int128 u128;
+
+namespace {
+
+struct MO {  // src/fringes.h:50-58 (139 packed bytes)
+  uint8_t nodes, anchorsets, startdeg, destdeg[5], list[5], anch[63], fcnt[63];
+};
+static_assert(sizeof(MO) == 139, "matching order layout");
+
+struct Graph {
+  int n;
+  long long m;
+  const long long* idx;
+  const int* adj;
+  int deg(int v) const { return (int)(idx[v + 1] - idx[v]); }
+  const int* beg(int v) const { return adj + idx[v]; }
+  const int* end(int v) const { return adj + idx[v + 1]; }
+};
+
+// Vertex bits of a 3-vertex core (src/fringeCount.cu:61-67).
+enum { IU = 1, IV = 2, IW = 4, IUV = 3, IUW = 5, IVW = 6, IUVW = 7 };
+
+// Binomial coefficient with the reference's u64 arithmetic: r = r*(n+1-i)/i,
+// wrapping multiply then truncating divide (src/fringeCount.cu:189-197).
+static inline u64 nck(int n, int k) {
+  k = std::min(k, n - k);
+  if (k < 0) return 0;
+  if (k == 0) return 1;
+  u64 r = (u64)n;
+  for (int i = 2; i <= k; i++) r = r * (u64)(n + 1 - i) / (u64)i;
+  return r;
+}
+
+static inline bool has(const Graph& g, int v, int x) {  // x in N(v)
+  return std::binary_search(g.beg(v), g.end(v), x);
+}
+
+static int common2(const Graph& g, int a, int b) {  // |N(a) & N(b)| by merge
+  const int *p = g.beg(a), *pe = g.end(a), *q = g.beg(b), *qe = g.end(b);
+  int c = 0;
+  while (p < pe && q < qe) {
+    if (*p < *q) p++;
+    else if (*q < *p) q++;
+    else { c++; p++; q++; }
+  }
+  return c;
+}
+
+// ---------------------------------------------------------------- 3-core formula
+// fc3: ways to place the fringes of the 7 anchor-set types into the 7 exclusive
+// Venn regions of a 3-vertex core (src/fringeCount.cu:233-327).  The loop nest
+// below visits the same (i,j,k,a,b,c,d) tuples and forms each term from the same
+// nCk factors as the reference; terms the reference skips with `break` are zero.
+static u64 fc3(const int fr[8], const int venn[8]) {
+  const int fuvw = fr[IUVW], fuv = fr[IUV], fuw = fr[IUW], fvw = fr[IVW];
+  const int fu = fr[IU], fv = fr[IV], fw = fr[IW];
+  int x_uvw = venn[IUVW], x_uv = venn[IUV], x_uw = venn[IUW], x_vw = venn[IVW];
+  const int x_u = venn[IU], x_v = venn[IV], x_w = venn[IW];
+  if (x_uvw < fuvw) return 0;
+  const u64 base = nck(x_uvw, fuvw);
+  x_uvw -= fuvw;
+  u64 total = 0;
+  // i of the uv-fringes go into the shared uvw region, the rest into uv
+  for (int i = std::min(x_uvw, fuv); i >= 0; i--) {
+    if (x_uv < fuv - i) break;
+    const u64 t1 = base * nck(x_uvw, i) * nck(x_uv, fuv - i);
+    const int r_uvw1 = x_uvw - i, r_uv = x_uv - (fuv - i);
+    for (int j = std::min(r_uvw1, fuw); j >= 0; j--) {
+      if (x_uw < fuw - j) break;
+      const u64 t2 = t1 * nck(r_uvw1, j) * nck(x_uw, fuw - j);
+      const int r_uvw2 = r_uvw1 - j, r_uw = x_uw - (fuw - j);
+      for (int k = std::min(r_uvw2, fvw); k >= 0; k--) {
+        if (x_vw < fvw - k) break;
+        const u64 t3 = t2 * nck(r_uvw2, k) * nck(x_vw, fvw - k);
+        const int r_uvw3 = r_uvw2 - k, r_vw = x_vw - (fvw - k);
+        // u-fringes: a from uvw, b from uv, c from uw, rest from u
+        for (int a = std::min(r_uvw3, fu); a >= 0; a--) {
+          const u64 ta = t3 * nck(r_uvw3, a);
+          const int r_uvw4 = r_uvw3 - a;
+          const int pool_v = r_uvw4 + r_vw;  // regions still open to v (uvw + vw)
+          for (int b = std::min(r_uv, fu - a); b >= 0; b--) {
+            const u64 tb = ta * nck(r_uv, b);
+            const int r_uv2 = r_uv - b;
+            for (int c = std::min(r_uw, fu - a - b); c >= 0; c--) {
+              if (x_u < fu - a - b - c) break;
+              const u64 tc = tb * nck(r_uw, c) * nck(x_u, fu - a - b - c);
+              const int r_uw2 = r_uw - c;
+              // v-fringes: d from (uvw + vw), rest from (uv + v)
+              for (int d = std::min(pool_v, fv); d >= 0; d--) {
+                if (r_uv2 + x_v < fv - d) break;
+                const u64 td = tc * nck(pool_v, d) * nck(r_uv2 + x_v, fv - d);
+                // w-fringes: everything still open to w
+                const int pool_w = (pool_v - d) + r_uw2 + x_w;
+                if (pool_w >= fw) total += td * nck(pool_w, fw);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  return total;
+}
+
+// Rotations and flips of the 3-core anchor counts, listed as the reference lists
+// them (triangle: src/fringeCount.cu:1291-1317, wedge: 1754-1780).
+static void rotate(const int q[8], int out[8]) {  // u<-v, v<-w, w<-u
+  out[IUVW] = q[IUVW]; out[IUV] = q[IVW]; out[IUW] = q[IUV]; out[IVW] = q[IUW];
+  out[IU] = q[IV]; out[IV] = q[IW]; out[IW] = q[IU]; out[0] = 0;
+}
+static void rotate2(const int q[8], int out[8]) {
+  out[IUVW] = q[IUVW]; out[IUV] = q[IUW]; out[IUW] = q[IVW]; out[IVW] = q[IUV];
+  out[IU] = q[IW]; out[IV] = q[IU]; out[IW] = q[IV]; out[0] = 0;
+}
+static void flip(const int f[8], int out[8]) {  // v<->w
+  out[IUVW] = f[IUVW]; out[IUV] = f[IUW]; out[IUW] = f[IUV]; out[IVW] = f[IVW];
+  out[IU] = f[IU]; out[IV] = f[IW]; out[IW] = f[IV]; out[0] = 0;
+}
+static int rotations3(const int f[8], int fr[6][8], bool wedge) {
+  int p = 0;
+  for (int i = 0; i < 8; i++) fr[0][i] = (i == 0) ? 0 : f[i];
+  p = 1;
+  const bool rot = wedge || (f[IU] != f[IV]) || (f[IU] != f[IW]) || (f[IUV] != f[IUW]) || (f[IUV] != f[IVW]);
+  if (!rot) return p;
+  rotate(fr[0], fr[1]);
+  rotate2(fr[0], fr[2]);
+  p = 3;
+  bool fl;
+  if (wedge) {
+    fl = (f[IV] != f[IW]) || (f[IUV] != f[IUW]);
+  } else {
+    fl = ((f[IV] != f[IW]) || (f[IUV] != f[IUW])) && ((f[IU] != f[IW]) || (f[IUV] != f[IVW])) &&
+         ((f[IU] != f[IV]) || (f[IUW] != f[IVW]));
+  }
+  if (fl) {
+    flip(f, fr[3]);
+    rotate(fr[3], fr[4]);
+    rotate2(fr[3], fr[5]);
+    p = 6;
+  }
+  return p;
+}
+
+// Sampling: top-level work items (the vertex that owns a worklist entry) are
+// processed only when v % stride == phase.  stride 1 processes everything.
+struct Sample {
+  int stride = 1, phase = 0;
+  bool take(int v) const { return stride <= 1 || (v % stride) == phase; }
+};
+
+// ---------------------------------------------------------------- vertex core
+// src/fringeCount.cu:2152-2191
+static u64 vertex_core(const MO& mo, const Graph& g, const Sample& s) {
+  if (mo.anchorsets == 0) return (u64)g.n;
+  if (mo.fcnt[0] == 1) return (u64)(g.m / 2);
+  const int t = mo.fcnt[0];
+  u64 tot = 0;
+#pragma omp parallel for reduction(+ : tot) schedule(dynamic, 4096)
+  for (int v = 0; v < g.n; v++)
+    if (s.take(v) && g.deg(v) >= t) tot += nck(g.deg(v), t);
+  return tot;
+}
+
+// ---------------------------------------------------------------- edge core
+// Worklist: undirected edges (u,v) with v < u by vertex id, pruned by degree
+// (init_wl_edge, src/fringeCount.cu:2054-2103); kernels triangle /
+// tailed_triangle / general_edge_core (1864-2051); dispatch edgeCore 2106-2144.
+static u64 edge_formula(int du, int dv, int c_uv, int f_u, int f_uv, int f_v) {
+  const int a_uv = c_uv - f_uv;
+  if (a_uv < 0) return 0;
+  const int c_u = du - 1 - c_uv, c_v = dv - 1 - c_uv;
+  const int bound = std::min(f_u, a_uv);
+  u64 acc = 0;
+  for (int j = 0; j <= bound; j++) {
+    const int k = f_u - j;
+    u64 term = nck(c_u, k) * nck(a_uv + c_v - j, f_v);
+    if (f_u != f_v) term += nck(c_v, k) * nck(a_uv + c_u - j, f_v);
+    acc += term * nck(a_uv, j);
+  }
+  return acc * nck(c_uv, f_uv);
+}
+
+static u64 edge_core(const MO& mo, const Graph& g, const Sample& s) {
+  int f[4] = {0, 0, 0, 0};
+  for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 3] = mo.fcnt[i];
+  const int f_u = std::min(f[1], f[2]), f_uv = f[3], f_v = std::max(f[1], f[2]);
+  const bool special = (f_uv == 1) && (f_u == 0 || f_v == 0);
+  const int lim1 = special ? 1 : f_u + f_uv;
+  const int lim2 = special ? 1 : f_u + f_uv + f_v;
+  u64 tot = 0;
+#pragma omp parallel for reduction(+ : tot) schedule(dynamic, 64)
+  for (int u = 0; u < g.n; u++) {
+    if (!s.take(u)) continue;
+    const int du = g.deg(u);
+    if (du <= lim1) continue;
+    const u64 cu = special ? nck(du - 2, f_v) : 0;
+    for (const int* p = g.beg(u); p < g.end(u) && *p < u; p++) {
+      const int v = *p, dv = g.deg(v);
+      if (!(dv > lim1 && du + dv > lim2)) continue;
+      if (special) {
+        // triangles w < v < u
+        const u64 c12 = cu + nck(dv - 2, f_v);
+        const int *a = g.beg(u), *ae = g.end(u), *b = g.beg(v), *be = g.end(v);
+        while (a < ae && b < be && *a < v && *b < v) {
+          if (*a < *b) a++;
+          else if (*b < *a) b++;
+          else {
+            if (f_u == 0 && f_v == 0) tot += 1;
+            else tot += c12 + nck(g.deg(*a) - 2, f_v);
+            a++; b++;
+          }
+        }
+      } else {
+        tot += edge_formula(du, dv, common2(g, u, v), f_u, f_uv, f_v);
+      }
+    }
+  }
+  return tot;
+}
+
+// ---------------------------------------------------------------- wedge core
+// src/fringeCount.cu:1381-1825.
+static u64 wedge_formula(int du, int dv, bool adj, int f_u, int f_uv, int f_v, int c_uv) {
+  // wedge(): endpoints "u","v" of a wedge whose centre is not counted in c_uv
+  const int a_uv = c_uv - f_uv;
+  if (a_uv < 0) return 0;
+  const int corr = adj ? 2 : 1;
+  const int a_u = du - (corr + c_uv), a_v = dv - (corr + c_uv);
+  const int bound = std::min(f_u, a_uv);
+  u64 sum = 0;
+  for (int j = 0; j <= bound; j++) {
+    const int k = f_u - j;
+    u64 term = nck(a_u, k) * nck(a_uv + a_v - j, f_v);
+    if (f_u != f_v) term += nck(a_v, k) * nck(a_uv + a_u - j, f_v);
+    sum += term * nck(a_uv, j);
+  }
+  return sum * nck(c_uv, f_uv);
+}
+
+// Exclusive Venn sizes of N(u),N(v),N(w) for a wedge or triangle centred at u,
+// before the caller's corrections (common3_wedge, src/fringeCount.cu:1480-1510).
+static void venn3_wedge(const Graph& g, int u, int v, int w, int p12, int venn[8]) {
+  int t13 = 0, t23 = 0, t123 = 0;
+  for (const int* p = g.beg(w); p < g.end(w); p++) {
+    const bool b13 = has(g, u, *p), b23 = has(g, v, *p);
+    t13 += b13; t23 += b23; t123 += (b13 && b23);
+  }
+  const int c123 = t123, c12 = p12 - c123, c13 = t13 - c123, c23 = t23 - c123;
+  venn[0] = 0;
+  venn[IU] = g.deg(u) - (p12 + c13);
+  venn[IV] = g.deg(v) - (p12 + c23);
+  venn[IW] = g.deg(w) - (c13 + c23 + c123);
+  venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
+}
+
+static u64 wedge_core(const MO& mo, const Graph& g, const Sample& s) {
+  int f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 7] = mo.fcnt[i];
+  if (mo.list[1] == 2) {  // centre is B: swap roles of A and B
+    std::swap(f[IU], f[IV]);
+    std::swap(f[IUW], f[IVW]);
+  }
+  const int min_u = f[IUVW] + f[IUV] + f[IUW] + f[IU] + 2;
+  const int min_v = f[IUVW] + f[IUV] + f[IVW] + f[IV] + 1;
+  const int min_w = f[IUVW] + f[IUW] + f[IVW] + f[IW] + 1;
+  const int sum3 = min_u + min_v + min_w;
+  const int sum2 = sum3 - std::max(std::max(min_u, min_v), min_w);
+  const int sum1 = std::min(std::min(min_u, min_v), min_w);
+  const int lim = std::min(min_v, min_w);
+  u64 tot = 0;
+  if (f[IUVW] == 0 && f[IUV] == 0 && f[IUW] == 0 && f[IU] == 0) {
+    // centre has no fringes: init_wl_specialized_wedge + wedgecore_specialized
+    const int fv = f[IV], fvw = f[IVW], fw = f[IW];
+#pragma omp parallel for reduction(+ : tot) schedule(dynamic, 16)
+    for (int u = 0; u < g.n; u++) {
+      if (!s.take(u) || g.deg(u) < 2) continue;
+      for (const int* pv = g.beg(u); pv < g.end(u); pv++) {
+        const int v = *pv, dv = g.deg(v);
+        if (dv < lim) continue;
+        const int thres = std::max(lim, min_v + min_w - dv);
+        for (const int* pw = g.beg(u); pw < g.end(u) && *pw < v; pw++) {
+          const int w = *pw, dw = g.deg(w);
+          if (dw < thres) continue;
+          const int c = common2(g, v, w) - 1;
+          tot += wedge_formula(dv, dw, has(g, w, v), fv, fvw, fw, c);
+        }
+      }
+    }
+    return tot;
+  }
+  int fr[6][8];
+  const int rot = rotations3(f, fr, true);
+#pragma omp parallel for reduction(+ : tot) schedule(dynamic, 16)
+  for (int u = 0; u < g.n; u++) {
+    if (!s.take(u)) continue;
+    const int du = g.deg(u);
+    if (du < sum1) continue;
+    const int th1u = std::max(sum1, sum2 - du);
+    for (const int* pv = g.beg(u); pv < g.end(u); pv++) {
+      const int v = *pv, dv = g.deg(v);
+      if (dv < th1u) continue;  // init_wl_wedge
+      const int p12 = common2(g, u, v);
+      const bool cond = (du >= min_u) && (dv >= lim);
+      const int thres1 = std::max(lim, sum2 - dv);
+      const int thres2 = std::max(std::max(sum1, sum3 - du - dv), std::max(sum2 - du, sum2 - dv));
+      for (const int* pw = g.beg(u); pw < g.end(u) && *pw < v; pw++) {
+        const int w = *pw, dw = g.deg(w);
+        if (dw < thres2) continue;
+        const bool tri = has(g, v, w);
+        int venn[8];
+        if (tri) {
+          if (!(u < w)) continue;
+          venn3_wedge(g, u, v, w, p12, venn);
+          venn[IUV]--; venn[IUW]--; venn[IVW]--;
+          for (int r = 0; r < rot; r++) tot += fc3(fr[r], venn);
+        } else {
+          if (!(cond && dw >= thres1)) continue;
+          venn3_wedge(g, u, v, w, p12, venn);
+          venn[IU] -= 2; venn[IVW]--;
+          tot += fc3(fr[0], venn);
+          if (rot > 3) tot += fc3(fr[3], venn);
+        }
+      }
+    }
+  }
+  return tot;
+}
+
+// ---------------------------------------------------------------- triangle core
+// src/fringeCount.cu:700-1373.  Vertex roles follow the reference's vertex
+// order: after its degree relabel (new id = rank of (degree, id) descending,
+// src/fringeCount.cu:1065-1085, 1247) when the relabel gates fire
+// (1237, 1342-1344), else the input ids.  key(x) reproduces "new id" order:
+// a smaller key is a smaller relabelled id.
+struct TriOrder {
+  bool relabel;
+  const Graph* g;
+  long long key(int x) const {
+    if (!relabel) return x;
+    return -(((long long)g->deg(x) << 32) + x);
+  }
+};
+
+static bool triangle_relabel_gate(const Graph& g) {
+  if (g.n <= 10000) return false;
+  if ((long long)g.n > g.m / 10) return false;
+  int maxd = 0;
+  for (int v = 0; v < g.n; v++) maxd = std::max(maxd, g.deg(v));
+  return maxd > 16;
+}
+
+static u64 triangle_core(const MO& mo, const Graph& g, const Sample& s) {
+  int f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 7] = mo.fcnt[i];
+  const int min_u = f[IUVW] + f[IUV] + f[IUW] + f[IU];
+  const int min_v = f[IUVW] + f[IUV] + f[IVW] + f[IV];
+  const int min_w = f[IUVW] + f[IUW] + f[IVW] + f[IW];
+  const int sum3 = min_u + min_v + min_w + 6;
+  const int sum2 = sum3 - (std::max(std::max(min_u, min_v), min_w) + 2);
+  const int sum1 = std::min(std::min(min_u, min_v), min_w) + 2;
+  int fr[6][8];
+  const int rot = rotations3(f, fr, false);
+  TriOrder ord{triangle_relabel_gate(g), &g};
+  const bool clique = (f[IUVW] == 1) && (f[IUV] + f[IUW] + f[IVW] == 0) &&
+                      ((f[IU] == 0) + (f[IV] == 0) + (f[IW] == 0) >= 2);
+  const int tails = f[IU] + f[IV] + f[IW];
+  u64 tot = 0;
+#pragma omp parallel for reduction(+ : tot) schedule(dynamic, 16)
+  for (int u = 0; u < g.n; u++) {
+    if (!s.take(u)) continue;
+    const int du = g.deg(u);
+    if (du < sum1) continue;
+    const int th1 = std::max(sum1, sum2 - du);
+    const long long ku = ord.key(u);
+    for (const int* pv = g.beg(u); pv < g.end(u); pv++) {
+      const int v = *pv, dv = g.deg(v);
+      const long long kv = ord.key(v);
+      if (!(kv < ku) || dv < th1) continue;  // init_wl_triangle: v before u
+      // w in N(u) & N(v) with w before v
+      std::vector<int> ws;
+      for (const int* pw = g.beg(u); pw < g.end(u); pw++)
+        if (ord.key(*pw) < kv && has(g, v, *pw)) ws.push_back(*pw);
+      if (clique) {
+        const u64 c12 = nck(du - 3, tails) + nck(dv - 3, tails);
+        for (int w : ws) {
+          const int dw = g.deg(w);
+          if (dw < 3) continue;
+          const long long kw = ord.key(w);
+          const u64 c123 = c12 + nck(dw - 3, tails);
+          for (const int* pq = g.beg(w); pq < g.end(w); pq++) {
+            const int q = *pq;
+            if (ord.key(q) < kw && has(g, u, q) && has(g, v, q))
+              tot += (tails == 0) ? 1 : c123 + nck(g.deg(q) - 3, tails);
+          }
+        }
+        continue;
+      }
+      const int p12 = common2(g, u, v);
+      const int thres2 = std::max(std::max(sum1, sum3 - du - dv), std::max(sum2 - du, sum2 - dv));
+      for (int w : ws) {
+        const int dw = g.deg(w);
+        if (dw < thres2) continue;
+        int t13 = 0, t23 = 0, t123 = 0;  // com3, src/fringeCount.cu:934-964
+        for (const int* pq = g.beg(w); pq < g.end(w); pq++) {
+          const bool b13 = has(g, u, *pq), b23 = has(g, v, *pq);
+          t13 += b13; t23 += b23; t123 += (b13 && b23);
+        }
+        int venn[8];
+        const int c123 = t123, c12 = p12 - (c123 + 1), c13 = t13 - (c123 + 1), c23 = t23 - (c123 + 1);
+        venn[0] = 0;
+        venn[IU] = du - (c12 + c13 + (c123 + 2));
+        venn[IV] = dv - (c12 + c23 + (c123 + 2));
+        venn[IW] = dw - (c13 + c23 + (c123 + 2));
+        venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
+        for (int r = 0; r < rot; r++) tot += fc3(fr[r], venn);
+      }
+    }
+  }
+  return tot;
+}
+
+// ---------------------------------------------------------------- general core
+// src/fringeCount.cu:345-692.  Ordered core matches are enumerated by the
+// matching order (mo.list / mo.destdeg); for each, the exclusive Venn region
+// sizes of the anchor vertices' neighbourhoods (commonX) feed a sum over all
+// placements of the fringes (functionX).
+struct GenCtx {
+  const MO* mo;
+  const Graph* g;
+  int k;            // core vertices
+  int anchors;      // bitmask of core vertices that anchor fringes
+  int nonanchors;
+  int stack[6];
+  int venn[64];
+};
+
+// commonX: histogram with prefix bitmaps, inclusion-exclusion correction, then
+// removal of the core vertices themselves (src/fringeCount.cu:345-405).
+static void venn_general(GenCtx& c) {
+  const Graph& g = *c.g;
+  for (int i = 0; i < 64; i++) c.venn[i] = 0;
+  for (int i = c.k - 1; i >= 0; i--) {
+    if (c.nonanchors & (1 << i)) continue;
+    const int vi = c.stack[i];
+    for (const int* p = g.beg(vi); p < g.end(vi); p++) {
+      int bmp = 1 << i;
+      for (int t = 0; t < i; t++) {
+        if (c.nonanchors & (1 << t)) continue;
+        if (has(g, c.stack[t], *p)) bmp |= 1 << t;
+      }
+      c.venn[bmp]++;
+    }
+  }
+  const int top = 1 << c.k;
+  for (int i = c.k - 2; i >= 0; i--) {
+    const int hi = 2 << i;
+    for (int j = 1 << i; j < hi; j++) {
+      int sum = 0;
+      for (int pos = j + hi; pos < top; pos += hi) sum += c.venn[pos];
+      c.venn[j] -= sum;
+    }
+  }
+  for (int l = 0; l < c.k; l++) {
+    const int x = c.stack[l];
+    int bmp = 0;
+    for (int t = 0; t < c.k; t++) {
+      if (c.nonanchors & (1 << t)) continue;
+      if (has(g, c.stack[t], x)) bmp |= 1 << t;
+    }
+    c.venn[bmp]--;
+  }
+}
+
+// functionX (src/fringeCount.cu:408-486): anchor sets are placed from the last to
+// the first; each set's fringes are spread over the regions that contain the
+// set, visited in increasing bitmap order, with the remainder going to the
+// region of all anchors.  Each placement contributes the product of
+// nCk(remaining region size, fringes put there).
+static u64 place(GenCtx& c, int asi, int idx, int remaining);
+static u64 place_set(GenCtx& c, int asi) {
+  const int anch = c.mo->anch[asi];
+  return place(c, asi, anch, c.mo->fcnt[asi]);
+}
+static u64 place(GenCtx& c, int asi, int idx, int remaining) {
+  const int top = c.anchors;
+  const int anch = c.mo->anch[asi];
+  if (idx == top) {
+    const u64 w = nck(c.venn[top], remaining);
+    if (w == 0) return 0;
+    if (asi == 0) return w;
+    c.venn[top] -= remaining;
+    const u64 r = w * place_set(c, asi - 1);
+    c.venn[top] += remaining;
+    return r;
+  }
+  const int next = (((idx | c.nonanchors) + 1) | anch) & ~c.nonanchors;
+  u64 s = 0;
+  for (int a = std::min(c.venn[idx], remaining); a >= 0; a--) {
+    const u64 w = nck(c.venn[idx], a);
+    if (w == 0) continue;
+    c.venn[idx] -= a;
+    s += w * place(c, asi, next, remaining - a);
+    c.venn[idx] += a;
+  }
+  return s;
+}
+
+static u64 gen_dfs(GenCtx& c, int level) {
+  // choose stack[level+1]
+  const MO& mo = *c.mo;
+  const Graph& g = *c.g;
+  const int list = mo.list[level];
+  const int first = __builtin_ctz(list);
+  const int src = c.stack[first];
+  u64 sum = 0;
+  for (const int* p = g.beg(src); p < g.end(src); p++) {
+    const int x = *p;
+    if (g.deg(x) < mo.destdeg[level]) continue;
+    bool ok = true;
+    for (int t = 0; t <= level && ok; t++) {
+      if (list & (1 << t)) {
+        if (t != first && !has(g, c.stack[t], x)) ok = false;
+      } else if (c.stack[t] == x) {
+        ok = false;
+      }
+    }
+    if (!ok) continue;
+    c.stack[level + 1] = x;
+    if (level + 1 == c.k - 1) {
+      venn_general(c);
+      sum += place_set(c, mo.anchorsets - 1);
+    } else {
+      sum += gen_dfs(c, level + 1);
+    }
+  }
+  return sum;
+}
+
+static u64 general_core(const MO& mo, const Graph& g, const Sample& s) {
+  int anchors = 0;
+  for (int i = 0; i < mo.anchorsets; i++) anchors |= mo.anch[i];
+  const int k = mo.nodes;
+  u64 tot = 0;
+#pragma omp parallel for reduction(+ : tot) schedule(dynamic, 4)
+  for (int u = 0; u < g.n; u++) {
+    if (!s.take(u) || g.deg(u) < mo.startdeg) continue;
+    GenCtx c;
+    c.mo = &mo; c.g = &g; c.k = k; c.anchors = anchors;
+    c.nonanchors = anchors ^ ((1 << k) - 1);
+    for (const int* p = g.beg(u); p < g.end(u); p++) {
+      const int v = *p;
+      if (g.deg(v) < mo.destdeg[0]) continue;  // init_wl_general
+      c.stack[0] = u;
+      c.stack[1] = v;
+      tot += gen_dfs(c, 1);
+    }
+  }
+  return tot;
+}
+
+// ---------------------------------------------------------------- dispatch
+// Pattern graph of a matching order: core vertices 0..k-1 with the mo.list
+// adjacency, then each anchor set's fringes (matchingOrder2ECLgraph,
+// src/fringeCount.cu:121-186).
+static void pattern_graph(const MO& mo, std::vector<long long>& idx, std::vector<int>& adj) {
+  int n = mo.nodes;
+  for (int i = 0; i < mo.anchorsets; i++) n += mo.fcnt[i];
+  std::vector<std::vector<int>> nb(n);
+  for (int i = 0; i < mo.nodes - 1; i++)
+    for (int j = 0; j <= i; j++)
+      if (mo.list[i] & (1 << j)) { nb[i + 1].push_back(j); nb[j].push_back(i + 1); }
+  int v = mo.nodes;
+  for (int i = 0; i < mo.anchorsets; i++)
+    for (int t = 0; t < mo.fcnt[i]; t++, v++)
+      for (int j = 0; j < 6; j++)
+        if (mo.anch[i] & (1 << j)) { nb[j].push_back(v); nb[v].push_back(j); }
+  idx.assign(n + 1, 0);
+  adj.clear();
+  for (int x = 0; x < n; x++) {
+    std::sort(nb[x].begin(), nb[x].end());
+    adj.insert(adj.end(), nb[x].begin(), nb[x].end());
+    idx[x + 1] = (long long)adj.size();
+  }
+}
+
+static u64 count_core(const MO& mo, const Graph& g, const Sample& s, int* core_type) {
+  if (mo.nodes == 1) { *core_type = 1; return vertex_core(mo, g, s); }
+  if (mo.nodes == 2) { *core_type = 2; return edge_core(mo, g, s); }
+  if (mo.nodes == 3) {
+    if (__builtin_popcount(mo.list[1]) == 1) { *core_type = 3; return wedge_core(mo, g, s); }
+    *core_type = 4;
+    return triangle_core(mo, g, s);
+  }
+  *core_type = 5;
+  return general_core(mo, g, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+// Count the occurrences of the pattern described by the 139-byte matching
+// order in graph (n, idx, adj) the way src/fringeCount.cu:2199-2262 does:
+// cores of 3 or more vertices are divided by the pattern's count in itself.
+// out[0] = final count, out[1] = raw total before the division,
+// out[2] = automorphism divisor, out[3] = core type (1 vertex .. 5 general).
+// stride/phase select a sample of top-level work items (stride 1 = all); the
+// automorphism divisor is always computed in full.
+int oracle_count(int n, const long long* idx, const int* adj, const unsigned char* mo_bytes, int stride,
+                 int phase, int threads, unsigned long long* out) {
+  MO mo;
+  memcpy(&mo, mo_bytes, sizeof(MO));
+  if (mo.nodes < 1 || mo.nodes > 6 || mo.anchorsets > 63) return -1;
+  if (threads > 0) omp_set_num_threads(threads);
+  Graph g{n, idx[n], idx, adj};
+  Sample s;
+  s.stride = stride < 1 ? 1 : stride;
+  s.phase = phase;
+  u64 aut = 1;
+  int ct = 0;
+  if (mo.nodes >= 3) {
+    std::vector<long long> pidx;
+    std::vector<int> padj;
+    pattern_graph(mo, pidx, padj);
+    const int pn = (int)pidx.size() - 1;
+    if (pn > n || pidx[pn] > g.m) {
+      out[0] = 0; out[1] = 0; out[2] = 0;
+      out[3] = (mo.nodes == 3) ? ((__builtin_popcount(mo.list[1]) == 1) ? 3 : 4) : 5;
+      return 0;
+    }
+    Graph pg{pn, pidx[pn], pidx.data(), padj.data()};
+    aut = count_core(mo, pg, Sample(), &ct);
+    // the reference divides by an int (src/fringeCount.cu:2213, 2230)
+    aut = (u64)(unsigned int)(int)aut;
+    if (aut == 0) return -2;
+  }
+  const u64 raw = count_core(mo, g, s, &ct);
+  out[0] = raw / aut;
+  out[1] = raw;
+  out[2] = aut;
+  out[3] = (u64)ct;
+  return 0;
+}
+
+// Per-call building blocks exposed for unit tests.
+unsigned long long oracle_nck(int n, int k) { return nck(n, k); }
+unsigned long long oracle_fc3(const int* fr8, const int* venn8) { return fc3(fr8, venn8); }
+int oracle_rotations(const int* f8, int wedge, int* fr48) {
+  int fr[6][8];
+  const int p = rotations3(f8, fr, wedge != 0);
+  memcpy(fr48, fr, sizeof(fr));
+  return p;
+}
+
+// ---------------------------------------------------------------- brute force
+// Independent check: number of injective maps of the pattern into the graph that
+// send every pattern edge to a graph edge, divided by the number of such maps of
+// the pattern into itself.  Exact (128-bit) for small graphs.
+namespace {
+struct Brute {
+  int pn;
+  std::vector<std::vector<int>> padj;  // pattern adjacency
+  std::vector<int> order;              // pattern vertices in search order
+  std::vector<int> parent;             // an earlier pattern neighbour, or -1
+  const Graph* g;
+  std::vector<int> map;
+  std::vector<char> used;
+  bool adj(int a, int b) const { return has(*g, a, b); }
+  u128 rec(int i) {
+    if (i == pn) return 1;
+    const int p = order[i];
+    u128 s = 0;
+    auto try_vertex = [&](int x) {
+      if (used[x]) return;
+      for (int q : padj[p]) {
+        const int mq = map[q];
+        if (mq >= 0 && !adj(mq, x)) return;
+      }
+      used[x] = 1; map[p] = x;
+      s += rec(i + 1);
+      used[x] = 0; map[p] = -1;
+    };
+    if (parent[i] >= 0) {
+      const int px = map[parent[i]];
+      for (const int* it = g->beg(px); it < g->end(px); it++) try_vertex(*it);
+    } else {
+      for (int x = 0; x < g->n; x++) try_vertex(x);
+    }
+    return s;
+  }
+};
+
+static u128 brute_embeddings(int pn, const int* pedges, int npe, const Graph& g) {
+  Brute b;
+  b.pn = pn;
+  b.padj.assign(pn, {});
+  for (int e = 0; e < npe; e++) {
+    const int a = pedges[2 * e], c = pedges[2 * e + 1];
+    if (a == c) continue;
+    if (std::find(b.padj[a].begin(), b.padj[a].end(), c) == b.padj[a].end()) {
+      b.padj[a].push_back(c);
+      b.padj[c].push_back(a);
+    }
+  }
+  // BFS order from the highest-degree vertex so each later vertex has a parent
+  std::vector<char> seen(pn, 0);
+  int start = 0;
+  for (int v = 0; v < pn; v++) if (b.padj[v].size() > b.padj[start].size()) start = v;
+  b.order.push_back(start);
+  b.parent.push_back(-1);
+  seen[start] = 1;
+  for (size_t h = 0; h < b.order.size(); h++) {
+    const int x = b.order[h];
+    for (int y : b.padj[x]) if (!seen[y]) { seen[y] = 1; b.order.push_back(y); b.parent.push_back(x); }
+  }
+  for (int v = 0; v < pn; v++) if (!seen[v]) { b.order.push_back(v); b.parent.push_back(-1); }
+  b.g = &g;
+  b.map.assign(pn, -1);
+  b.used.assign(g.n, 0);
+  return b.rec(0);
+}
+}  // namespace
+
+// out[0..1] = count (low, high 64 bits), out[2..3] = |Aut(P)| (low, high).
+int oracle_bruteforce(int n, const long long* idx, const int* adj, int pn, const int* pedges, int npe,
+                      unsigned long long* out) {
+  Graph g{n, idx[n], idx, adj};
+  std::vector<long long> pidx;
+  std::vector<int> padjv;
+  {
+    std::vector<std::vector<int>> nb(pn);
+    for (int e = 0; e < npe; e++) {
+      const int a = pedges[2 * e], c = pedges[2 * e + 1];
+      if (a == c) continue;
+      nb[a].push_back(c); nb[c].push_back(a);
+    }
+    pidx.assign(pn + 1, 0);
+    for (int v = 0; v < pn; v++) {
+      std::sort(nb[v].begin(), nb[v].end());
+      nb[v].erase(std::unique(nb[v].begin(), nb[v].end()), nb[v].end());
+      padjv.insert(padjv.end(), nb[v].begin(), nb[v].end());
+      pidx[v + 1] = (long long)padjv.size();
+    }
+  }
+  Graph pg{pn, pidx[pn], pidx.data(), padjv.data()};
+  const u128 aut = brute_embeddings(pn, pedges, npe, pg);
+  const u128 emb = brute_embeddings(pn, pedges, npe, g);
+  if (aut == 0) return -1;
+  const u128 c = emb / aut;
+  out[0] = (u64)c; out[1] = (u64)(c >> 64);
+  out[2] = (u64)aut; out[3] = (u64)(aut >> 64);
+  return 0;
+}
+
+}  // extern "C"

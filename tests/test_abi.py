@@ -1,0 +1,93 @@
+"""C ABI surface and host-side logic of libfsgc (no GPU needed)."""
+import os
+import random
+import re
+
+import numpy as np
+import pytest
+
+import fsgc
+import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "fsgc.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fsgc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = fsgc.lib()
+    names = declared_symbols()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(L, name), name
+
+
+def test_device_binomial_arithmetic_on_host():
+    # the magic-number division used on the device, evaluated on the host
+    L = fsgc.lib()
+    rng = random.Random(1)
+    for _ in range(20000):
+        d = rng.randint(2, 63)
+        x = rng.getrandbits(64) if rng.random() < 0.8 else rng.choice([0, 1, d - 1, d, (1 << 64) - 1, (1 << 63)])
+        assert L.fsgc_div_small_host(x, d) == x // d
+    for _ in range(5000):
+        k = rng.randint(0, 31)
+        n = rng.choice([rng.randint(-2, 60), rng.randint(0, 20000), rng.randint(0, 2**31 - 1)])
+        assert L.fsgc_nck_host(n, k) == oracle.nck(n, k), (n, k)
+
+
+def test_generators_are_deterministic_and_valid():
+    a = fsgc.gen_rmat(10, 8, seed=3)
+    b = fsgc.gen_rmat(10, 8, seed=3)
+    assert np.array_equal(a.nindex, b.nindex) and np.array_equal(a.nlist, b.nlist)
+    assert fsgc.validate(a)[0] == 0
+    er = fsgc.gen_er(2000, 15000, seed=4)
+    assert er.m == 30000 and fsgc.validate(er)[0] == 0
+    cl = fsgc.gen_chung_lu(3000, 10.0, 2.4, seed=5)
+    assert fsgc.validate(cl)[0] == 0
+    assert cl.degrees().max() > 5 * cl.degrees().mean()
+
+
+def test_egr_round_trip_and_errors(tmp_path):
+    g = fsgc.gen_er(500, 2000, seed=2)
+    p = str(tmp_path / "g.egr")
+    fsgc.egr_write(p, g)
+    h = fsgc.egr_read(p)
+    assert np.array_equal(g.nindex, h.nindex) and np.array_equal(g.nlist, h.nlist)
+    raw = open(p, "rb").read()
+    # the ECLgraph layout: int32 n, int32 m, nindex[n+1], nlist[m]
+    hdr = np.frombuffer(raw[:8], dtype=np.int32)
+    assert hdr[0] == 500 and hdr[1] == 4000 and len(raw) == 8 + 4 * 501 + 4 * 4000
+    (tmp_path / "t.egr").write_bytes(raw[: len(raw) // 2])
+    with pytest.raises(fsgc.FsgcError):
+        fsgc.egr_read(str(tmp_path / "t.egr"))
+    with pytest.raises(fsgc.FsgcError):
+        fsgc.egr_read(str(tmp_path / "missing.egr"))
+
+
+def test_validate_catches_broken_inputs():
+    g = fsgc.csr_from_edges(4, [(0, 1), (1, 2), (2, 3)])
+    assert fsgc.validate(g)[0] == 0
+    bad = fsgc.Graph(g.nindex.copy(), g.nlist.copy())
+    bad.nlist[0] = 0  # self loop on vertex 0
+    assert fsgc.validate(bad)[0] != 0
+    asym = fsgc.Graph(np.array([0, 1, 1], np.int64), np.array([1], np.int32))
+    assert "symmetric" in fsgc.validate(asym)[1]
+
+
+def test_edges_to_csr_cleans_input():
+    g = fsgc.csr_from_edges(5, [(0, 1), (1, 0), (2, 2), (3, 4), (0, 1), (4, 3)])
+    assert g.m == 4 and list(g.nlist) == [1, 0, 4, 3]
+
+
+def test_context_without_gpu_fails_loudly():
+    import subprocess
+    r = subprocess.run(["nvidia-smi"], capture_output=True) if os.path.exists("/usr/bin/nvidia-smi") else None
+    if r is not None and r.returncode == 0:
+        pytest.skip("a GPU is present")
+    with pytest.raises(fsgc.FsgcError):
+        fsgc.Context(0)
