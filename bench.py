@@ -1,0 +1,352 @@
+"""Benchmark: pattern counts per second on RMAT scale 22 (the reference's
+eight single-pattern workload), on N GPUs of one node.
+
+One step = one pass of the counting path over the workload: the graph's
+loader passes (degree orientation, triangle supports) plus the eight counts,
+each result read back to the host.
+
+  value   inputs resident in HBM (a device copy of the raw CSR) when the timed
+          region starts; CUDA events on the context stream
+  e2e     the same step through the C ABI from pinned host buffers, the CSR
+          upload and the result read-back inside the timed region
+  --impl reference
+          the reference's algorithm on the host cores: the oracle's CPU
+          restatement of the reference's per-match formulas (the reference has
+          no CPU path of its own and its GPU binary cannot be built for the
+          Arm host), on a bounded sample of each pattern's work items,
+          extrapolated to the whole workload
+
+Multi-GPU: replicas only (each rank counts the whole workload on its own
+GPU); value = all ranks' patterns / the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fringe-sgc_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+WORKLOAD = {
+    "wedge_1_on_centre": (4, [(0, 1), (0, 2), (0, 3)]),
+    "wedge_2_on_centre": (5, [(0, 1), (0, 2), (0, 3), (0, 4)]),
+    "wedge_4_on_centre": (7, [(0, 1), (0, 2), (0, 3), (0, 4), (0, 5), (0, 6)]),
+    "wedge_1_on_each_end": (5, [(0, 1), (0, 2), (1, 3), (2, 4)]),
+    "triangle_3_on_one": (6, [(0, 1), (1, 2), (0, 2), (0, 3), (0, 4), (0, 5)]),
+    "4cycle_opposite": (6, [(0, 1), (1, 2), (2, 3), (3, 0), (0, 4), (2, 5)]),
+    "4clique_3_distinct": (7, [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3), (0, 4), (1, 5), (2, 6)]),
+    "edge_5_5": (12, [(0, 1)] + [(0, i) for i in range(2, 7)] + [(1, i) for i in range(7, 12)]),
+}
+RMAT = dict(scale=22, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=20251203)
+METRIC = "pattern counts/s (RMAT-22, 8 single patterns)"
+UNIT = "patterns/s"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.lines:
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload_graph():
+    import fsgc
+    t = time.time()
+    g = fsgc.gen_rmat(RMAT["scale"], RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], RMAT["seed"])
+    return g, time.time() - t
+
+
+def matching_orders():
+    import fsgc
+    return [(name, fsgc.preprocess(n, e)) for name, (n, e) in WORKLOAD.items()]
+
+
+def wedge_bytes(g):
+    """Algorithmic bytes of the wedge-pair kernel: every centre u lists each
+    pair of its neighbours once (4 bytes per neighbour-list entry read)."""
+    d = g.degrees().astype(np.float64)
+    return 4.0 * float((d * (d - 1) / 2).sum())
+
+
+def kernel_bytes(name, core, g):
+    d = g.degrees().astype(np.float64)
+    if core == 1:
+        return 4.0 * g.n  # degree array
+    if core == 2 and name == "triangle_3_on_one":
+        return 12.0 * g.n  # per-vertex triangle counts + degrees
+    if core == 2:
+        return 12.0 * g.m / 2  # oriented edge endpoints + support
+    if core == 3:
+        return wedge_bytes(g)
+    return None
+
+
+def run_gpu(args, rank, world):
+    import fsgc
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    ctx = fsgc.Context(dev)
+    g, gen_s = workload_graph()
+    mos = matching_orders()
+    tasks_of = lambda gid: [(gid, mo) for _, mo in mos]  # noqa: E731
+    # raw CSR resident in HBM for the device-resident measurement
+    import ctypes as C
+    L = fsgc.lib()
+    cudart = None
+    d_idx = C.c_void_p()
+    d_adj = C.c_void_p()
+    try:
+        import torch
+        t_idx = torch.from_numpy(g.nindex).to(f"cuda:{dev}")
+        t_adj = torch.from_numpy(g.nlist).to(f"cuda:{dev}")
+        torch.cuda.synchronize(dev)
+        d_idx, d_adj = t_idx.data_ptr(), t_adj.data_ptr()
+    except ImportError:
+        raise SystemExit("torch is needed for the device-resident copy of the input")
+    # pinned host copy for e2e
+    h = g.as_host_csr()
+    L.fsgc_host_csr_pin(C.byref(h))
+
+    def step_device():
+        gid = ctx.upload_device(g.n, g.m, d_idx, d_adj)
+        ctx.prepare(gid)
+        res = ctx.count_batch(tasks_of(gid))
+        ctx.release(gid)
+        return res
+
+    def step_host():
+        gid = ctx.upload(g)
+        res = ctx.count_batch(tasks_of(gid))
+        ctx.release(gid)
+        return res
+
+    barrier = (lambda: __import__("torch").distributed.barrier()) if world > 1 else (lambda: None)
+    for _ in range(args.warmup):
+        ref_res = step_device()
+    # timed: device-resident
+    launches0 = ctx.launches
+    barrier()
+    ctx.synchronize()
+    per_step = []
+    per_task = np.zeros(len(mos))
+    prep_ms = []
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            ctx.timer_start()
+            gid = ctx.upload_device(g.n, g.m, d_idx, d_adj)
+            ctx.prepare(gid)
+            prep_ms.append(ctx.timer_stop())
+            res = ctx.count_batch(tasks_of(gid))
+            ctx.release(gid)
+            per_task += np.array([r.device_ms for r in res])
+            per_step.append(prep_ms[-1] + sum(r.device_ms for r in res))
+            for a, b in zip(res, ref_res):
+                assert a.count == b.count, "count changed between steps"
+    ctx.synchronize()
+    barrier()
+    launches = ctx.launches - launches0
+    t_dev = sum(per_step) / 1000.0
+    # e2e through the C ABI from pinned host memory, wall clock
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res_h = step_host()
+    t_e2e = time.perf_counter() - t0
+    barrier()
+    for a, b in zip(res_h, ref_res):
+        assert a.count == b.count
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev, t_e2e = float(tt[0]), float(tt[1])
+    out = {
+        "per_task_ms": {name: per_task[i] / args.steps for i, (name, _) in enumerate(mos)},
+        "prep_ms": statistics.mean(prep_ms),
+        "counts": {name: int(r.count) for (name, _), r in zip(mos, ref_res)},
+        "cores": {name: int(r.core_type) for (name, _), r in zip(mos, ref_res)},
+        "t_dev": t_dev, "t_e2e": t_e2e, "launches": launches, "clocks": clk.summary(), "gen_s": gen_s,
+        "graph": {"n": g.n, "m": g.m, "max_degree": int(g.degrees().max())},
+    }
+    return out, g, mos, ctx
+
+
+def cpu_sample(g, mos, budget_s, threads):
+    """Time the oracle on a sample of each pattern's top-level work items
+    (every stride-th vertex), growing the sample until it takes ~budget_s."""
+    import oracle
+    per = budget_s / len(mos)
+    est, samples = 0.0, {}
+    for name, mo in mos:
+        stride = 1 << 16
+        while True:
+            t0 = time.perf_counter()
+            oracle.count(g.nindex, g.nlist, mo.to_bytes(), stride=stride, phase=stride // 2 + 1, threads=threads)
+            t = time.perf_counter() - t0
+            if t >= per / 4 or stride == 1:
+                break
+            stride = max(1, stride // 4)
+        est += t * stride
+        samples[name] = stride
+    return est, samples
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fsgc", choices=["fsgc", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        g, _ = workload_graph()
+        mos = matching_orders()
+        for _ in range(args.warmup):
+            cpu_sample(g, mos, args.cpu_budget / 4, threads)
+        ests = []
+        for _ in range(args.steps):
+            est, samples = cpu_sample(g, mos, args.cpu_budget, threads)
+            ests.append(est)
+        t = statistics.mean(ests)
+        value = len(mos) / t
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1000, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+                "config": {"workload": "RMAT scale 22, edge factor 16, (a,b,c,d)=(.57,.19,.19,.05), 8 patterns",
+                           "patterns": list(WORKLOAD)},
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": "every stride-th top-level vertex per pattern, strides " +
+                                           json.dumps(samples) + ", time x stride"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    out, g, mos, ctx = run_gpu(args, rank, world)
+    if rank != 0:
+        ctx.close()
+        if world > 1:
+            __import__("torch").distributed.destroy_process_group()
+        return
+    n_pat = len(mos) * world
+    value = n_pat * args.steps / out["t_dev"]
+    e2e = n_pat * args.steps / out["t_e2e"]
+    peak, peak_kind = load_peaks()
+    # dominant kernel: the task with the largest device time
+    dom = max(out["per_task_ms"], key=out["per_task_ms"].get)
+    core = out["cores"][dom]
+    alg = kernel_bytes(dom, core, g)
+    ms = out["per_task_ms"][dom]
+    roof = None
+    if alg is not None and ms > 0:
+        ach = alg / (ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "traffic": None, "kernel": dom, "kernel_ms": round(ms, 3),
+                "algorithmic_bytes": alg, "peak_kind": peak_kind}
+    cpu = None
+    if world == 1 and args.cpu_budget > 0:
+        est, samples = cpu_sample(g, mos, args.cpu_budget, os.cpu_count() or 1)
+        cpu = {"value": len(mos) / est, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": "oracle on every stride-th top-level vertex per pattern, strides " + json.dumps(samples)}
+    h2d = 8 * (g.n + 1) + 4 * g.m
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": out["t_dev"] * 1000 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": "RMAT scale 22, edge factor 16, (a,b,c,d)=(.57,.19,.19,.05), 8 single patterns",
+                   "n": g.n, "m_directed": g.m, "max_degree": out["graph"]["max_degree"],
+                   "patterns": list(WORKLOAD), "parallelism": f"replicas x{world}",
+                   "l2": "inputs (0.5 GB CSR) larger than L2, and L2 flushed before every timed step",
+                   "prep_ms": round(out["prep_ms"], 3),
+                   "per_pattern_ms": {k: round(v, 3) for k, v in out["per_task_ms"].items()},
+                   "counts": out["counts"]},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * len(mos)},
+        "gpu_launches": out["launches"],
+        "clocks": out["clocks"],
+    }
+    print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        __import__("torch").distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

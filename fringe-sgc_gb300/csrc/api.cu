@@ -34,6 +34,9 @@ struct fsgc_ctx {
   int slot_cap = 0;
   std::vector<cudaEvent_t> events;
   std::map<std::string, u64> aut_cache;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  void* flush_buf = nullptr;
+  size_t flush_bytes = 0;
 };
 
 namespace {
@@ -320,6 +323,9 @@ void fsgc_ctx_destroy(fsgc_ctx* c) {
   for (auto& kv : c->graphs) free_graph(kv.second);
   c->graphs.clear();
   for (auto e : c->events) cudaEventDestroy(e);
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
+  cudaFree(c->flush_buf);
   cudaFree(c->work.small);
   cudaFree(c->work.pairs.ptr);
   cudaFree(c->d_slots);
@@ -332,6 +338,56 @@ const char* fsgc_ctx_last_error(const fsgc_ctx* c) { return c ? c->err.c_str() :
 void* fsgc_ctx_stream(fsgc_ctx* c) { return c ? (void*)c->stream : nullptr; }
 uint64_t fsgc_ctx_launches(const fsgc_ctx* c) { return c ? c->launches : 0; }
 
+int fsgc_ctx_timer_start(fsgc_ctx* c) {
+  if (!c) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  if (!c->t0) {
+    CK(cudaEventCreate(&c->t0), "event creation");
+    CK(cudaEventCreate(&c->t1), "event creation");
+  }
+  CK(cudaEventRecord(c->t0, c->stream), "event record");
+  return FSGC_OK;
+}
+
+int fsgc_ctx_timer_stop(fsgc_ctx* c, double* ms) {
+  if (!c || !ms || !c->t0) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  CK(cudaEventRecord(c->t1, c->stream), "event record");
+  CK(cudaEventSynchronize(c->t1), "event sync");
+  float f = 0;
+  CK(cudaEventElapsedTime(&f, c->t0, c->t1), "event time");
+  *ms = f;
+  return FSGC_OK;
+}
+
+int fsgc_ctx_flush_l2(fsgc_ctx* c, size_t bytes) {
+  if (!c) return FSGC_EINVAL;
+  if (bytes == 0) bytes = (size_t)512 << 20;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  if (c->flush_bytes < bytes) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->flush_buf);
+    c->flush_buf = nullptr;
+    c->flush_bytes = 0;
+    CK(cudaMalloc(&c->flush_buf, bytes), "flush buffer");
+    c->flush_bytes = bytes;
+  }
+  static unsigned char pattern = 0;
+  pattern++;
+  CK(cudaMemsetAsync(c->flush_buf, pattern, bytes, c->stream), "flush");
+  return FSGC_OK;
+}
+
+int fsgc_ctx_synchronize(fsgc_ctx* c) {
+  if (!c) return FSGC_EINVAL;
+  cudaSetDevice(c->device);
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  return FSGC_OK;
+}
+
 int fsgc_graph_from_csr(fsgc_ctx* c, int n, int64_t m, const int64_t* nindex, const int32_t* nlist, int* gid) {
   if (!c || !gid || n < 1 || m < 0 || !nindex || (m > 0 && !nlist)) return fail(c, FSGC_EINVAL, "bad graph arguments");
   if (nindex[0] != 0 || nindex[n] != m) return fail(c, FSGC_EINVAL, "offsets must start at 0 and end at m");
@@ -342,6 +398,7 @@ int fsgc_graph_from_csr(fsgc_ctx* c, int n, int64_t m, const int64_t* nindex, co
   DevGraph* g = nullptr;
   int st = upload_graph(c, n, m, (const long long*)nindex, nlist, false, &g);
   if (st != FSGC_OK) return st;
+  CK(cudaStreamSynchronize(c->stream), "graph upload");
   *gid = c->next_gid++;
   c->graphs[*gid] = g;
   return FSGC_OK;
@@ -386,6 +443,17 @@ int fsgc_graph_release(fsgc_ctx* c, int gid) {
   cudaStreamSynchronize(c->stream);
   free_graph(it->second);
   c->graphs.erase(it);
+  return FSGC_OK;
+}
+
+int fsgc_graph_prepare(fsgc_ctx* c, int gid) {
+  if (!c) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DevGraph* g = find_graph(c, gid);
+  if (!g) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", gid);
+  const int st = fsgc::prepare_graph(*g, c->stream, &c->launches, c->work.small);
+  if (st != FSGC_OK) return fail(c, st, "graph preparation failed: %s", cudaGetErrorString(cudaGetLastError()));
   return FSGC_OK;
 }
 

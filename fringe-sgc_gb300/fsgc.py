@@ -93,9 +93,14 @@ def lib():
             "fsgc_graph_from_device_csr": (I, [P, I, I64, P, P, C.POINTER(C.c_int)]),
             "fsgc_graph_load_egr": (I, [P, C.c_char_p, C.POINTER(C.c_int)]),
             "fsgc_graph_release": (I, [P, I]),
+            "fsgc_graph_prepare": (I, [P, I]),
             "fsgc_graph_info_get": (I, [P, I, C.POINTER(GraphInfo)]),
             "fsgc_count": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(Result)]),
             "fsgc_count_batch": (I, [P, C.POINTER(Task), I, C.POINTER(Result)]),
+            "fsgc_ctx_timer_start": (I, [P]),
+            "fsgc_ctx_timer_stop": (I, [P, C.POINTER(C.c_double)]),
+            "fsgc_ctx_flush_l2": (I, [P, C.c_size_t]),
+            "fsgc_ctx_synchronize": (I, [P]),
             "fsgc_nck_host": (C.c_ulonglong, [I, I]),
             "fsgc_div_small_host": (C.c_ulonglong, [C.c_ulonglong, C.c_uint]),
         }
@@ -245,6 +250,20 @@ class Context:
     def stream(self):
         return lib().fsgc_ctx_stream(self.ptr)
 
+    def timer_start(self):
+        _check(lib().fsgc_ctx_timer_start(self.ptr), "timer_start", self.ptr)
+
+    def timer_stop(self):
+        ms = C.c_double()
+        _check(lib().fsgc_ctx_timer_stop(self.ptr, C.byref(ms)), "timer_stop", self.ptr)
+        return ms.value
+
+    def flush_l2(self, nbytes=0):
+        _check(lib().fsgc_ctx_flush_l2(self.ptr, nbytes), "flush_l2", self.ptr)
+
+    def synchronize(self):
+        _check(lib().fsgc_ctx_synchronize(self.ptr), "synchronize", self.ptr)
+
     def upload(self, g):
         gid = C.c_int()
         _check(lib().fsgc_graph_from_csr(self.ptr, g.n, g.m, g.nindex.ctypes.data, g.nlist.ctypes.data,
@@ -264,6 +283,9 @@ class Context:
 
     def release(self, gid):
         _check(lib().fsgc_graph_release(self.ptr, gid), "graph_release", self.ptr)
+
+    def prepare(self, gid):
+        _check(lib().fsgc_graph_prepare(self.ptr, gid), "graph_prepare", self.ptr)
 
     def info(self, gid):
         gi = GraphInfo()

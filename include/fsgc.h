@@ -122,6 +122,12 @@ const char* fsgc_ctx_last_error(const fsgc_ctx* ctx);
 void* fsgc_ctx_stream(fsgc_ctx* ctx);
 /* Number of this library's kernels launched by the context so far. */
 uint64_t fsgc_ctx_launches(const fsgc_ctx* ctx);
+/* Benchmark support: CUDA events on the context stream around a region, and a
+ * write of `bytes` (0 = 512 MiB, larger than the 126 MB L2) to evict caches. */
+int fsgc_ctx_timer_start(fsgc_ctx* ctx);
+int fsgc_ctx_timer_stop(fsgc_ctx* ctx, double* ms);
+int fsgc_ctx_flush_l2(fsgc_ctx* ctx, size_t bytes);
+int fsgc_ctx_synchronize(fsgc_ctx* ctx);
 
 /* ---- resident graphs (CSR upload + loader: src/fringeCount.cu:2286-2297) ---- */
 
@@ -134,6 +140,10 @@ int fsgc_graph_from_device_csr(fsgc_ctx* ctx, int n, int64_t m, const int64_t* d
                                int* gid);
 int fsgc_graph_load_egr(fsgc_ctx* ctx, const char* path, int* gid);
 int fsgc_graph_release(fsgc_ctx* ctx, int gid);
+/* Runs the loader's derived passes now (degree orientation, triangle supports)
+ * instead of on the first count that needs them (the reference's relabel and
+ * worklist builders, src/fringeCount.cu:1221-1288, 617-663, 1167-1218). */
+int fsgc_graph_prepare(fsgc_ctx* ctx, int gid);
 
 typedef struct fsgc_graph_info {
   int32_t n;

@@ -1,0 +1,188 @@
+"""GPU counts against the oracle, bit for bit (count, raw u64 total, divisor,
+core type), through the C ABI.  Graphs are small enough for the oracle to
+finish in seconds and include hubs whose degrees make the reference's u64
+binomials wrap, so the wrapping arithmetic itself is compared."""
+import numpy as np
+import pytest
+
+import fsgc
+import oracle
+from helpers import EXTRA, WORKLOAD, complete_graph, golden_cases, star_graph
+
+pytestmark = pytest.mark.gpu
+
+
+def hub_graph(n=3000, hub=2000, extra=8000, seed=3):
+    rng = np.random.default_rng(seed)
+    pairs = [(0, i) for i in range(1, hub + 1)]
+    a = rng.integers(1, n, size=extra)
+    b = rng.integers(1, n, size=extra)
+    pairs += list(zip(a.tolist(), b.tolist()))
+    return fsgc.csr_from_edges(n, pairs)
+
+
+GRAPHS = {
+    "er300": lambda: fsgc.gen_er(300, 2400, 7),
+    "rmat10": lambda: fsgc.gen_rmat(10, 8, seed=5),
+    "cl2000": lambda: fsgc.gen_chung_lu(2000, 8.0, 2.2, 9),
+    "k12": lambda: complete_graph(12),
+    "star300": lambda: star_graph(300),
+    "hub3000": hub_graph,
+}
+# General cores (4-6 core vertices) enumerate every ordered core match and every
+# fringe placement; on graphs with hubs that takes the oracle (and the
+# reference's algorithm) minutes per pattern, so they run on the sparse graphs.
+ALL_CORES = {"er300", "k12", "star300"}
+
+RANDOM = [c for c in golden_cases("random") if c["mo"] is not None]
+PATTERNS = {**WORKLOAD, **EXTRA}
+PATTERNS.update({f"pre{k}": fsgc.predefined_pattern(k) for k in range(1, 31)})
+
+
+def mos():
+    out = [(name, fsgc.preprocess(n, e)) for name, (n, e) in PATTERNS.items()]
+    out += [(c["name"], fsgc.MatchingOrder.from_bytes(bytes.fromhex(c["mo"]))) for c in RANDOM[:60]]
+    return out
+
+
+_cache = {}
+
+
+def graph(name):
+    if name not in _cache:
+        _cache[name] = GRAPHS[name]()
+    return _cache[name]
+
+
+def check(ctx, g, gid, name, mo, threads=0):
+    r = ctx.count(gid, mo)
+    o = oracle.count(g.nindex, g.nlist, mo.to_bytes(), threads=threads)
+    got = (r.count, r.raw_total, r.automorphisms, r.core_type)
+    want = (o["count"], o["raw"], o["aut"], o["core"])
+    assert got == want, (name, got, want)
+
+
+@pytest.mark.parametrize("gname", list(GRAPHS))
+def test_counts_match_oracle(ctx, gname):
+    g = graph(gname)
+    gid = ctx.upload(g)
+    try:
+        for name, mo in mos():
+            if gname not in ALL_CORES and mo.nodes >= 4:
+                continue
+            check(ctx, g, gid, name, mo)
+    finally:
+        ctx.release(gid)
+
+
+def test_wrapping_patterns_on_hub(ctx):
+    """Many fringes on one anchor: nck(2000, k) wraps for k >= 7."""
+    g = graph("hub3000")
+    gid = ctx.upload(g)
+    try:
+        deg = g.degrees()
+        assert deg.max() >= 2000
+        pats = {
+            "star7": (8, [(0, i) for i in range(1, 8)]),
+            "star12": (13, [(0, i) for i in range(1, 13)]),
+            "edge_8_3": EXTRA["edge_8_3"],
+            "edge_7_7": (16, [(0, 1)] + [(0, i) for i in range(2, 9)] + [(1, i) for i in range(9, 16)]),
+            "triangle_7_on_one": (10, [(0, 1), (1, 2), (0, 2)] + [(0, i) for i in range(3, 10)]),
+            "wedge_ends_7_1": (11, [(0, 1), (0, 2)] + [(1, i) for i in range(3, 10)] + [(2, 10)]),
+            "wedge_centre_7": (11, [(0, 1), (0, 2)] + [(0, i) for i in range(3, 10)] + [(1, 10), (2, 10)]),
+            "triangle_core_7": (12, [(0, 1), (1, 2), (0, 2)] + [e for i in range(3, 10) for e in ((0, i), (1, i))]
+                                + [(1, 10), (2, 10), (0, 11), (2, 11)]),
+        }
+        for name, (n, e) in pats.items():
+            check(ctx, g, gid, name, fsgc.preprocess(n, e))
+    finally:
+        ctx.release(gid)
+
+
+def test_batch_equals_single_counts(ctx):
+    g = graph("rmat10")
+    g2 = graph("er300")
+    a, b = ctx.upload(g), ctx.upload(g2)
+    try:
+        ms = [mo for _, mo in mos()[:40] if mo.nodes <= 3]
+        tasks = [(a, mo) for mo in ms] + [(b, mo) for mo in ms]
+        res = ctx.count_batch(tasks)
+        for (gid, mo), r in zip(tasks, res):
+            s = ctx.count(gid, mo)
+            assert (r.count, r.raw_total, r.automorphisms) == (s.count, s.raw_total, s.automorphisms)
+    finally:
+        ctx.release(a)
+        ctx.release(b)
+
+
+def test_edge_cases(ctx):
+    tri = fsgc.preprocess(3, [(0, 1), (1, 2), (0, 2)])
+    k4p3 = fsgc.preprocess(*WORKLOAD["4clique_3_distinct"])
+    # graph without edges, isolated vertices, a single edge
+    for g in (fsgc.Graph(np.zeros(6, np.int64), np.zeros(0, np.int32)), fsgc.csr_from_edges(2, [(0, 1)]),
+              fsgc.csr_from_edges(50, [(0, 1), (1, 2), (0, 2)])):
+        gid = ctx.upload(g)
+        for name, (n, e) in {**WORKLOAD, **EXTRA}.items():
+            check(ctx, g, gid, name, fsgc.preprocess(n, e))
+        r = ctx.count(gid, k4p3)
+        assert r.count == 0
+        ctx.release(gid)
+    # pattern larger than the graph: the reference returns 0 early
+    g = complete_graph(5)
+    gid = ctx.upload(g)
+    r = ctx.count(gid, k4p3)
+    assert r.count == 0 and (r.flags & 1)
+    assert ctx.count(gid, tri).count == 10
+    ctx.release(gid)
+    with pytest.raises(fsgc.FsgcError):
+        ctx.count(12345, tri)
+
+
+def test_config1_full_size(ctx):
+    """ER n=20,000, m=200,000 with the triangle + 2 single fringes pattern,
+    against the oracle and the brute-force enumerator."""
+    g = fsgc.gen_er(20000, 200000, seed=1)
+    n, e = WORKLOAD["er_triangle_2fringes"]
+    mo = fsgc.preprocess(n, e)
+    gid = ctx.upload(g)
+    try:
+        r = ctx.count(gid, mo)
+        o = oracle.count(g.nindex, g.nlist, mo.to_bytes())
+        assert (r.count, r.raw_total) == (o["count"], o["raw"])
+        b, _ = oracle.bruteforce(g.nindex, g.nlist, n, e)
+        assert r.count == b
+    finally:
+        ctx.release(gid)
+
+
+def test_device_resident_input(ctx):
+    torch = pytest.importorskip("torch")
+    g = graph("rmat10")
+    d_idx = torch.from_numpy(g.nindex).cuda()
+    d_adj = torch.from_numpy(g.nlist).cuda()
+    torch.cuda.synchronize()
+    gid = ctx.upload_device(g.n, g.m, d_idx.data_ptr(), d_adj.data_ptr())
+    try:
+        mo = fsgc.preprocess(*WORKLOAD["4clique_3_distinct"])
+        check(ctx, g, gid, "k4p3", mo)
+    finally:
+        ctx.release(gid)
+
+
+def test_cli_drop_in(tmp_path):
+    import os
+    import re
+    import subprocess
+    g = graph("rmat10")
+    p = str(tmp_path / "g.egr")
+    fsgc.egr_write(p, g)
+    exe = os.path.dirname(fsgc.LIB_PATH)
+    n, e = WORKLOAD["triangle_3_on_one"]
+    args = [str(n)] + [str(x) for ed in e for x in ed]
+    subprocess.run([os.path.join(exe, "fringePreprocess"), *args], cwd=tmp_path, check=True, capture_output=True)
+    r = subprocess.run([os.path.join(exe, "fringeCount"), p, "motif.mo"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert re.search(r"runtime: \d+\.\d{6} s", r.stdout)
+    cnt = int(re.search(r"(-?\d+) occurrences", r.stdout).group(1))
+    o = oracle.count(g.nindex, g.nlist, (tmp_path / "motif.mo").read_bytes())
+    assert cnt % (1 << 64) == o["count"]
