@@ -122,6 +122,11 @@ int upload_graph(fsgc_ctx* c, int n, long long m, const long long* off, const in
     return cuda_fail(c, e, "graph upload");
   }
   g->bytes = sizeof(long long) * ((size_t)n + 1) + sizeof(int) * ((size_t)m + (size_t)n);
+  const int st = fsgc::graph_degrees(*g, c->stream, &c->launches, c->work.small);
+  if (st != FSGC_OK) {
+    free_graph(g);
+    return fail(c, st, "degree pass failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
   *out = g;
   return FSGC_OK;
 }
@@ -266,8 +271,9 @@ int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
   for (int t = 0; t < nt; t++) {
     const u64 raw = jobs[t].host_only ? jobs[t].host_value : c->h_slots[t];
     res[t].raw_total = raw;
-    res[t].automorphisms = aut[t];
-    res[t].count = raw / aut[t];
+    // no divisor is computed when the pattern does not fit the graph
+    res[t].automorphisms = (res[t].flags & FSGC_FLAG_PATTERN_TOO_LARGE) ? 0 : aut[t];
+    res[t].count = (res[t].flags & FSGC_FLAG_PATTERN_TOO_LARGE) ? 0 : raw / aut[t];
     res[t].core_type = jobs[t].core_type;
     float ms = 0;
     cudaEventElapsedTime(&ms, c->events[t], c->events[t + 1]);

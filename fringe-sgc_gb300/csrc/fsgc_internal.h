@@ -73,6 +73,7 @@ struct DevWork {
 struct Launcher;  // forward
 
 // Entry points implemented in prep.cu / count.cu.
+int graph_degrees(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_scratch_u64);
 int prepare_graph(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_scratch_u64);
 int ensure_vertex_triangles(DevGraph& g, cudaStream_t s, uint64_t* launches);
 void upload_div_magic();

@@ -239,17 +239,25 @@ static int grid_for(long long work, int tpb, int per_sm) {
     if (e__ != cudaSuccess) return FSGC_ECUDA;    \
   } while (0)
 
+// Degrees and the maximum degree; run when a graph becomes resident.
+int graph_degrees(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_u64) {
+  int* d_max = reinterpret_cast<int*>(d_u64);
+  FSGC_TRY(cudaMemsetAsync(d_max, 0, sizeof(int), s));
+  degree_kernel<<<grid_for(g.n, kTPB, 8), kTPB, 0, s>>>(g.n, g.off, g.deg, d_max);
+  *launches += 1;
+  int maxd = 0;
+  FSGC_TRY(cudaMemcpyAsync(&maxd, d_max, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FSGC_TRY(cudaStreamSynchronize(s));
+  FSGC_TRY(cudaGetLastError());
+  g.maxdeg = maxd;
+  return FSGC_OK;
+}
+
 int prepare_graph(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_u64) {
   if (g.prepared) return FSGC_OK;
   const int n = g.n;
   const long long me = g.m / 2;
-  // degrees and maximum degree
-  int* d_max = reinterpret_cast<int*>(d_u64);
-  FSGC_TRY(cudaMemsetAsync(d_max, 0, sizeof(int), s));
-  degree_kernel<<<grid_for(n, kTPB, 8), kTPB, 0, s>>>(n, g.off, g.deg, d_max);
-  int maxd = 0;
-  FSGC_TRY(cudaMemcpyAsync(&maxd, d_max, sizeof(int), cudaMemcpyDeviceToHost, s));
-  *launches += 1;
+  const int maxd = g.maxdeg;
   // oriented CSR
   long long* odeg = nullptr;
   const long long ntiles = ((long long)n + kScanTile - 1) / kScanTile;
@@ -283,7 +291,6 @@ int prepare_graph(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_u64) {
   FSGC_TRY(cudaFreeAsync(tiles, s));
   FSGC_TRY(cudaStreamSynchronize(s));
   FSGC_TRY(cudaGetLastError());
-  g.maxdeg = maxd;
   g.triangles = (long long)tri;
   // the reference relabels (and so orders triangle roles by degree) only for
   // n > 10000, n <= m/10 and maximum degree > 16

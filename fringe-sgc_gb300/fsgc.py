@@ -41,7 +41,6 @@ class Result(C.Structure):
 
 
 class Task(C.Structure):
-    _pack_ = 1
     _fields_ = [("gid", C.c_int32), ("mo", MatchingOrder)]
 
 

@@ -91,3 +91,12 @@ def test_context_without_gpu_fails_loudly():
         pytest.skip("a GPU is present")
     with pytest.raises(fsgc.FsgcError):
         fsgc.Context(0)
+
+
+def test_struct_layouts_match_the_header():
+    import ctypes as C
+    # fsgc_matching_order is the reference's 139-byte MatchingOrder; fsgc_task
+    # pads to 4-byte alignment (int32 gid first)
+    assert C.sizeof(fsgc.MatchingOrder) == 139
+    assert C.sizeof(fsgc.Task) == 144
+    assert C.sizeof(fsgc.Result) == 40
