@@ -334,6 +334,7 @@ void fsgc_ctx_destroy(fsgc_ctx* c) {
   cudaFree(c->flush_buf);
   cudaFree(c->work.small);
   cudaFree(c->work.pairs.ptr);
+  cudaFree(c->work.tri.ptr);
   cudaFree(c->d_slots);
   cudaFreeHost(c->h_slots);
   if (c->stream) cudaStreamDestroy(c->stream);

@@ -180,6 +180,7 @@ struct TriParams {
   int mode;   // 0 general, 1 4-clique, 2 tailed 4-clique
   int tails;
   int relabel;  // roles by (deg, id) order (1) or by id (0)
+  int kmax;     // largest out-degree (bitmap kernel)
   Rot3 rot;
 };
 
@@ -328,6 +329,115 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
   block_sum_to(acc, slot);
 }
 
+// Triangle core, general placements: one block per vertex a, handling every
+// triangle whose lowest (deg, id) vertex is a.  For each out-neighbour b_i of a
+// the block builds the bitmap M_i of N(a) & N(b_i) over the positions of N(a)
+// (one warp ballot per 32 neighbours).  Then a pair (b_i, b_j) is a triangle
+// iff bit pos(b_j) of M_i is set, |N(a) & N(b_i)| = popc(M_i), and the triple
+// overlap |N(a) & N(b_i) & N(b_j)| = popc(M_i & M_j) -- a few word operations
+// per triangle instead of an intersection of full neighbour lists.
+__global__ void __launch_bounds__(256) triangle_bitmap_kernel(GView g, TriParams p, int* __restrict__ queue,
+                                                              unsigned* __restrict__ bits_all, long long bits_per_block,
+                                                              u64* __restrict__ slot) {
+  extern __shared__ int s_dyn[];
+  __shared__ int s_a;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  unsigned* bits = bits_all + (size_t)blockIdx.x * (size_t)bits_per_block;
+  const int kmax = p.kmax;
+  int* outl = s_dyn;            // out-neighbours of a
+  int* pos = s_dyn + kmax;      // their positions in N(a)
+  int* rowpop = s_dyn + 2 * kmax;  // |N(a) & N(b_i)|
+  u64 acc = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_a = atomicAdd(queue, 1);
+    __syncthreads();
+    const int a = s_a;
+    if (a >= g.n) break;
+    const long long ob = g.ooff[a];
+    const int k = (int)(g.ooff[a + 1] - ob);
+    const int da = g.deg[a];
+    if (k >= 2 && da >= p.sum1) {
+      const int W = (da + 31) >> 5;
+      const int* Na = g.adj + g.off[a];
+      for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        const int b = g.oadj[ob + i];
+        outl[i] = b;
+        pos[i] = lower_bound_dev(Na, da, b);
+      }
+      // bitmaps: row i = N(a) & N(b_i), skipped when the edge closes no triangle
+      for (int i = warp; i < k; i += nwarp) {
+        const unsigned sup = g.osup[ob + i];
+        int cnt = 0;
+        if (sup) {
+          const int b = g.oadj[ob + i];
+          const int* Nb = g.adj + g.off[b];
+          const int db = g.deg[b];
+          for (int w = 0; w < W; w++) {
+            const int x = w * 32 + lane;
+            const bool hit = (x < da) && bsearch_has(Nb, db, __ldg(Na + x));
+            const unsigned word = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0) bits[(size_t)i * W + w] = word;
+            cnt += __popc(word);
+          }
+        }
+        if (lane == 0) rowpop[i] = cnt;
+      }
+      __syncthreads();
+      // pairs (i, j), i < j: warp per row, lanes over j
+      for (int i = warp; i < k - 1; i += nwarp) {
+        if (rowpop[i] == 0) continue;
+        const unsigned* Mi = bits + (size_t)i * W;
+        const int bi = outl[i], di = g.deg[bi];
+        for (int j = i + 1 + lane; j < k; j += 32) {
+          const int pj = pos[j];
+          if (!((Mi[pj >> 5] >> (pj & 31)) & 1u)) continue;
+          const int bj = outl[j], dj = g.deg[bj];
+          const unsigned* Mj = bits + (size_t)j * W;
+          int c123 = 0;
+          for (int w = 0; w < W; w++) c123 += __popc(Mi[w] & Mj[w]);
+          // support of edge (b_i, b_j): slot in the out-list of the lower one
+          const bool i_low = (di < dj) || (di == dj && bi < bj);
+          const int lo = i_low ? bi : bj, hi = i_low ? bj : bi;
+          const long long lb = g.ooff[lo];
+          const int sl = bsearch_pos(g.oadj + lb, (int)(g.ooff[lo + 1] - lb), hi);
+          const int s_ij = (int)g.osup[lb + sl];
+          // roles u (latest), v, w (earliest) in the reference's vertex order
+          const int xv[3] = {a, bi, bj};
+          const int dx[3] = {da, di, dj};
+          long long kx[3];
+          for (int t = 0; t < 3; t++) kx[t] = tri_key(xv[t], dx[t], p.relabel);
+          int ord[3] = {0, 1, 2};
+          if (kx[ord[0]] < kx[ord[1]]) { int t = ord[0]; ord[0] = ord[1]; ord[1] = t; }
+          if (kx[ord[1]] < kx[ord[2]]) { int t = ord[1]; ord[1] = ord[2]; ord[2] = t; }
+          if (kx[ord[0]] < kx[ord[1]]) { int t = ord[0]; ord[0] = ord[1]; ord[1] = t; }
+          // pairwise overlaps by vertex slot: 0 = a, 1 = b_i, 2 = b_j
+          const int sup01 = rowpop[i], sup02 = rowpop[j], sup12 = s_ij;
+          auto sup = [&](int x, int y) {
+            const int s = x + y;  // 1 -> (0,1), 2 -> (0,2), 3 -> (1,2)
+            return s == 1 ? sup01 : (s == 2 ? sup02 : sup12);
+          };
+          const int iu = ord[0], iv = ord[1], iw = ord[2];
+          const int du = dx[iu], dv = dx[iv], dw = dx[iw];
+          const int th1 = max(p.sum1, p.sum2 - du);
+          const int th2 = max(max(p.sum1, p.sum3 - du - dv), max(p.sum2 - du, p.sum2 - dv));
+          if (!((du >= p.sum1) && (dv >= th1) && (dw >= th2))) continue;
+          const int p12 = sup(iu, iv), t13 = sup(iu, iw), t23 = sup(iv, iw);
+          const int c12 = p12 - (c123 + 1), c13 = t13 - (c123 + 1), c23 = t23 - (c123 + 1);
+          int venn[8];
+          venn[0] = 0;
+          venn[IU] = du - (c12 + c13 + (c123 + 2));
+          venn[IV] = dv - (c12 + c23 + (c123 + 2));
+          venn[IW] = dw - (c13 + c23 + (c123 + 2));
+          venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
+          for (int r = 0; r < p.rot.count; r++) acc += fc3(p.rot.fr[r], venn);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  block_sum_to(acc, slot);
+}
+
 // ------------------------------------------------------------- wedge core
 struct WedgeParams {
   int f_v, f_vw, f_w;  // fringes of the larger-id endpoint, both, the other
@@ -341,7 +451,7 @@ struct WedgeParams {
 // centre count C: C * wedge(v, w, C - 1).
 __global__ void __launch_bounds__(512) wedge_pair_kernel(GView g, WedgeParams p, unsigned* __restrict__ cnt_all,
                                                          int* __restrict__ touched_all, int* __restrict__ queue,
-                                                         u64* __restrict__ slot) {
+                                                         int dv_min, u64* __restrict__ slot) {
   __shared__ int s_v, s_nt;
   unsigned* cnt = cnt_all + (size_t)blockIdx.x * (size_t)g.n;
   int* touched = touched_all + (size_t)blockIdx.x * (size_t)g.n;
@@ -356,7 +466,7 @@ __global__ void __launch_bounds__(512) wedge_pair_kernel(GView g, WedgeParams p,
     const int v = s_v;
     if (v >= g.n) break;
     const int dv = g.deg[v];
-    if (dv >= p.lim) {
+    if (dv >= p.lim && dv >= dv_min) {
       const int thres = max(p.lim, p.minsum - dv);
       const long long vb = g.off[v];
       for (int t = warp; t < dv; t += nwarp) {
@@ -382,6 +492,156 @@ __global__ void __launch_bounds__(512) wedge_pair_kernel(GView g, WedgeParams p,
         const bool vw = bsearch_has(Nv, dv, w);
         acc += (u64)C * wedge_formula(dv, g.deg[w], vw, p.f_v, p.f_vw, p.f_w, (int)C - 1);
       }
+    }
+    __syncthreads();
+  }
+  block_sum_to(acc, slot);
+}
+
+// Same sum as wedge_pair_kernel, with the centre counts of endpoint v kept in
+// shared memory: the ids w < v are swept in chunks of kWCh; per chunk every
+// centre u in N(v) contributes the segment of N(u) inside the chunk (a cursor
+// per centre walks each sorted list once), the segment lengths are prefix-
+// summed so that all threads share the chunk's elements evenly, counts go to
+// shared-memory counters, and only the touched counters are evaluated and
+// cleared.  Chunks no centre reaches are skipped.  Endpoints of degree above
+// kWDvMax are left to wedge_pair_kernel.
+constexpr int kWCh = 16384;
+constexpr int kWDvMax = 2048;
+constexpr int kWThreads = 1024;
+
+struct WedgeChunkSmem {
+  unsigned cnt[kWCh];
+  unsigned short touched[kWCh];
+  unsigned adjbits[kWCh / 32];
+  long long cur[kWDvMax];
+  long long lim[kWDvMax];
+  int pre[kWDvMax + 1];
+  int warp_tmp[32];
+  int nt;
+  int v;
+  int lo;
+};
+
+__global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, WedgeParams p, int* __restrict__ queue,
+                                                                   u64* __restrict__ slot) {
+  extern __shared__ unsigned char s_raw[];
+  WedgeChunkSmem& S = *reinterpret_cast<WedgeChunkSmem*>(s_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  for (int i = tid; i < kWCh; i += blockDim.x) S.cnt[i] = 0;
+  for (int i = tid; i < kWCh / 32; i += blockDim.x) S.adjbits[i] = 0;
+  u64 acc = 0;
+  for (;;) {
+    if (tid == 0) {
+      S.v = atomicAdd(queue, 1);
+      S.nt = 0;
+      S.lo = 0;
+    }
+    __syncthreads();
+    const int v = S.v;
+    if (v >= g.n) break;
+    const int dv = g.deg[v];
+    if (dv < p.lim || dv > kWDvMax) {
+      __syncthreads();
+      continue;
+    }
+    const int thres = max(p.lim, p.minsum - dv);
+    const long long vb = g.off[v];
+    const int* Nv = g.adj + vb;
+    for (int t = tid; t < dv; t += blockDim.x) {
+      const int u = __ldg(Nv + t);
+      S.cur[t] = g.off[u];
+      S.lim[t] = g.off[u + 1];
+    }
+    int cv = 0;  // cursor into N(v) for the adjacency marks
+    __syncthreads();
+    while (S.lo < v) {
+      const int lo = S.lo;
+      const int hi = min(lo + kWCh, v);
+      // segment of each centre's list inside [lo, hi)
+      for (int t = tid; t < dv; t += blockDim.x) {
+        const long long c = S.cur[t];
+        S.pre[t] = lower_bound_dev(g.adj + c, (int)(S.lim[t] - c), hi);
+      }
+      __syncthreads();
+      // exclusive scan of the segment lengths (dv <= kWDvMax <= 2 * blockDim)
+      {
+        int x0 = (2 * tid < dv) ? S.pre[2 * tid] : 0;
+        int x1 = (2 * tid + 1 < dv) ? S.pre[2 * tid + 1] : 0;
+        int sum = x0 + x1, inc = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, inc, o);
+          if (lane >= o) inc += y;
+        }
+        if (lane == 31) S.warp_tmp[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+          int wv = (lane < nwarp) ? S.warp_tmp[lane] : 0, wi = wv;
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+          }
+          if (lane < nwarp) S.warp_tmp[lane] = wi - wv;
+        }
+        __syncthreads();
+        const int ex = S.warp_tmp[warp] + inc - sum;
+        if (2 * tid < dv) S.pre[2 * tid] = ex;
+        if (2 * tid + 1 < dv) S.pre[2 * tid + 1] = ex + x0;
+        if (2 * tid + 1 == dv - 1 || 2 * tid == dv - 1) S.pre[dv] = ex + sum;
+      }
+      // adjacency marks for N(v) inside the chunk (chunks may have been skipped)
+      const int cs = cv + lower_bound_dev(Nv + cv, dv - cv, lo);
+      const int cend = cs + lower_bound_dev(Nv + cs, dv - cs, hi);
+      for (int i = cs + tid; i < cend; i += blockDim.x) {
+        const int o = __ldg(Nv + i) - lo;
+        atomicOr(&S.adjbits[o >> 5], 1u << (o & 31));
+      }
+      __syncthreads();
+      const int L = S.pre[dv];
+      for (int e = tid; e < L; e += blockDim.x) {
+        // centre t owning element e: last t with pre[t] <= e
+        int a = 0, b = dv;
+        while (b - a > 1) {
+          const int mid = (a + b) >> 1;
+          if (S.pre[mid] <= e) a = mid;
+          else b = mid;
+        }
+        const int w = __ldg(g.adj + S.cur[a] + (e - S.pre[a]));
+        const unsigned old = atomicAdd(&S.cnt[w - lo], 1u);
+        if (old == 0) S.touched[atomicAdd(&S.nt, 1)] = (unsigned short)(w - lo);
+      }
+      __syncthreads();
+      const int nt = S.nt;
+      for (int q = tid; q < nt; q += blockDim.x) {
+        const int o = S.touched[q];
+        const unsigned C = S.cnt[o];
+        S.cnt[o] = 0;
+        const int w = lo + o;
+        const int dw = g.deg[w];
+        if (dw >= thres) {
+          const bool vw = (S.adjbits[o >> 5] >> (o & 31)) & 1u;
+          acc += (u64)C * wedge_formula(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1);
+        }
+      }
+      __syncthreads();  // adjbits and pre are still read above
+      for (int i = tid; i < kWCh / 32; i += blockDim.x) S.adjbits[i] = 0;
+      // advance the cursors and find the next id any centre still reaches
+      int nxt = 0x7fffffff;
+      for (int t = tid; t < dv; t += blockDim.x) {
+        const long long c = S.cur[t] + (S.pre[t + 1] - S.pre[t]);
+        S.cur[t] = c;
+        if (c < S.lim[t]) nxt = min(nxt, __ldg(g.adj + c));
+      }
+      nxt = __reduce_min_sync(0xffffffffu, nxt);
+      cv = cend;
+      __syncthreads();
+      if (tid == 0) {
+        S.nt = 0;
+        S.lo = v;
+      }
+      __syncthreads();
+      if (lane == 0) atomicMin(&S.lo, max(hi, nxt));
+      __syncthreads();
     }
     __syncthreads();
   }
@@ -714,6 +974,22 @@ int grid_for(long long work, int tpb, int per_sm) {
   return (int)std::max(1LL, std::min(want, cap));
 }
 
+int ensure_plain_scratch(Scratch& sc, size_t need, cudaStream_t s) {
+  if (sc.bytes >= need) return FSGC_OK;
+  if (sc.ptr) {
+    cudaStreamSynchronize(s);
+    cudaFree(sc.ptr);
+    sc.ptr = nullptr;
+    sc.bytes = 0;
+  }
+  if (cudaMalloc(&sc.ptr, need) != cudaSuccess) {
+    cudaGetLastError();
+    return FSGC_ENOMEM;
+  }
+  sc.bytes = need;
+  return FSGC_OK;
+}
+
 // Pair-counter scratch for the wedge core: `blocks` rows of n counters plus
 // `blocks` rows of n touched-list entries.  Counters are zero whenever no
 // kernel is running (each launch clears what it touched), so they are only
@@ -813,6 +1089,15 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
     const int lim = std::min(min_v, min_w);
     if (f[IUVW] == 0 && f[IUV] == 0 && f[IUW] == 0 && f[IU] == 0) {
       WedgeParams wp{f[IV], f[IVW], f[IW], lim, min_v + min_w};
+      {
+        int* q1 = reinterpret_cast<int*>(work.small + 7);
+        cudaMemsetAsync(q1, 0, sizeof(int), s);
+        const size_t smem = sizeof(WedgeChunkSmem);
+        cudaFuncSetAttribute(wedge_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        wedge_chunk_kernel<<<sm_count(), kWThreads, smem, s>>>(gv, wp, q1, job.d_slot);
+        *launches += 1;
+      }
+      if (G.maxdeg <= kWDvMax) return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
       // dense per-block pair counters + touched lists, bounded to 16 GiB
       const size_t per_block = (size_t)G.n * (sizeof(unsigned) + sizeof(int));
       int blocks = sm_count() * 2;
@@ -824,7 +1109,7 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
       cudaMemsetAsync(queue, 0, sizeof(int), s);
       unsigned* cnt = reinterpret_cast<unsigned*>(work.pairs.ptr);
       int* touched = reinterpret_cast<int*>(cnt + (size_t)blocks * G.n);
-      wedge_pair_kernel<<<blocks, 512, 0, s>>>(gv, wp, cnt, touched, queue, job.d_slot);
+      wedge_pair_kernel<<<blocks, 512, 0, s>>>(gv, wp, cnt, touched, queue, kWDvMax + 1, job.d_slot);
       *launches += 1;
       return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
     }
@@ -851,11 +1136,29 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
     tp.tails = f[IU] + f[IV] + f[IW];
     tp.mode = clique ? (tp.tails == 0 ? 1 : 2) : 0;
     tp.relabel = G.tri_relabel ? 1 : 0;
+    tp.kmax = (int)G.max_outdeg;
     rotations3(f, false, tp.rot);
-    if (me > 0) {
+    if (me == 0) return FSGC_OK;
+    const size_t smem = (size_t)3 * sizeof(int) * (size_t)std::max(1, tp.kmax);
+    if (tp.mode == 0 && smem <= (size_t)96 * 1024) {
+      // bitmap kernel: rows of ceil(deg/32) words per out-neighbour, per block
+      const long long per_block = std::max(1LL, G.max_bitmap_words);
+      int blocks = sm_count() * 4;
+      const size_t budget = (size_t)8 << 30;
+      blocks = (int)std::max<size_t>(1, std::min<size_t>((size_t)blocks, budget / (sizeof(unsigned) * (size_t)per_block)));
+      const size_t need = sizeof(unsigned) * (size_t)per_block * (size_t)blocks;
+      st = ensure_plain_scratch(work.tri, need, s);
+      if (st != FSGC_OK) return st;
+      int* queue = reinterpret_cast<int*>(work.small + 6);
+      cudaMemsetAsync(queue, 0, sizeof(int), s);
+      if (smem > 48 * 1024)
+        cudaFuncSetAttribute(triangle_bitmap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      triangle_bitmap_kernel<<<blocks, 256, smem, s>>>(gv, tp, queue, reinterpret_cast<unsigned*>(work.tri.ptr),
+                                                        per_block, job.d_slot);
+    } else {
       triangle_core_kernel<<<grid_for(me, TPB, 8), TPB, 0, s>>>(gv, tp, job.d_slot);
-      *launches += 1;
     }
+    *launches += 1;
     return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
   }
 

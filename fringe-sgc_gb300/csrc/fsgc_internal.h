@@ -41,6 +41,8 @@ struct DevGraph {
   int* osrc = nullptr;
   unsigned* osup = nullptr;
   long long triangles = -1;
+  long long max_outdeg = 0;        // largest oriented out-degree
+  long long max_bitmap_words = 0;  // max over v of outdeg(v) * ceil(deg(v) / 32)
   u64* vtri2 = nullptr;  // lazily
   // the reference's degree-relabel gate for the triangle core
   // (src/fringeCount.cu:1237, 1342-1344): vertex roles follow (deg, id) order
@@ -68,6 +70,7 @@ struct Scratch {
 struct DevWork {
   u64* small = nullptr;  // 32 u64
   Scratch pairs;
+  Scratch tri;
 };
 
 struct Launcher;  // forward

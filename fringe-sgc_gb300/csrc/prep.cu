@@ -202,6 +202,24 @@ __global__ void triangle_support_kernel(GView g, unsigned* __restrict__ osup, u6
   block_sum_to(tot, tri_total);
 }
 
+// largest out-degree and largest out-degree * ceil(deg / 32) (bitmap rows)
+__global__ void outdeg_stats_kernel(GView g, unsigned long long* __restrict__ stats) {
+  unsigned long long k1 = 0, k2 = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x) {
+    const unsigned long long k = (unsigned long long)(g.ooff[v + 1] - g.ooff[v]);
+    k1 = max(k1, k);
+    k2 = max(k2, k * (unsigned long long)((g.deg[v] + 31) >> 5));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    k1 = max(k1, __shfl_down_sync(0xffffffffu, k1, o));
+    k2 = max(k2, __shfl_down_sync(0xffffffffu, k2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(stats, k1);
+    atomicMax(stats + 1, k2);
+  }
+}
+
 __global__ void vertex_triangle_kernel(GView g, u64* __restrict__ vtri2) {
   const long long me = g.m / 2;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < me; j += (long long)gridDim.x * blockDim.x) {
@@ -285,13 +303,19 @@ int prepare_graph(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_u64) {
     triangle_support_kernel<<<grid_for(me, kTPB, 8), kTPB, 0, s>>>(v, g.osup, d_tri);
     *launches += 1;
   }
-  u64 tri = 0;
-  FSGC_TRY(cudaMemcpyAsync(&tri, d_tri, sizeof(u64), cudaMemcpyDeviceToHost, s));
+  u64* d_stats = d_u64 + 2;
+  FSGC_TRY(cudaMemsetAsync(d_stats, 0, 2 * sizeof(u64), s));
+  outdeg_stats_kernel<<<grid_for(n, kTPB, 8), kTPB, 0, s>>>(v, d_stats);
+  *launches += 1;
+  u64 stats[3] = {0, 0, 0};
+  FSGC_TRY(cudaMemcpyAsync(stats, d_tri, 3 * sizeof(u64), cudaMemcpyDeviceToHost, s));
   FSGC_TRY(cudaFreeAsync(odeg, s));
   FSGC_TRY(cudaFreeAsync(tiles, s));
   FSGC_TRY(cudaStreamSynchronize(s));
   FSGC_TRY(cudaGetLastError());
-  g.triangles = (long long)tri;
+  g.triangles = (long long)stats[0];
+  g.max_outdeg = (long long)stats[1];
+  g.max_bitmap_words = (long long)stats[2];
   // the reference relabels (and so orders triangle roles by degree) only for
   // n > 10000, n <= m/10 and maximum degree > 16
   g.tri_relabel = (n > 10000) && !((long long)n > g.m / 10) && (maxd > 16);

@@ -12,11 +12,13 @@ from helpers import EXTRA, WORKLOAD, complete_graph, golden_cases, star_graph
 pytestmark = pytest.mark.gpu
 
 
-def hub_graph(n=3000, hub=2000, extra=8000, seed=3):
+def hub_graph(n=3000, hub=2000, extra=8000, seed=3, hub_id=0):
+    """A star of `hub` leaves around vertex hub_id plus random edges."""
     rng = np.random.default_rng(seed)
-    pairs = [(0, i) for i in range(1, hub + 1)]
-    a = rng.integers(1, n, size=extra)
-    b = rng.integers(1, n, size=extra)
+    leaves = [x for x in range(n) if x != hub_id][:hub]
+    pairs = [(hub_id, i) for i in leaves]
+    a = rng.integers(0, n, size=extra)
+    b = rng.integers(0, n, size=extra)
     pairs += list(zip(a.tolist(), b.tolist()))
     return fsgc.csr_from_edges(n, pairs)
 
@@ -75,9 +77,12 @@ def test_counts_match_oracle(ctx, gname):
         ctx.release(gid)
 
 
-def test_wrapping_patterns_on_hub(ctx):
-    """Many fringes on one anchor: nck(2000, k) wraps for k >= 7."""
-    g = graph("hub3000")
+@pytest.mark.parametrize("hub_id", [0, 2999])
+def test_wrapping_patterns_on_hub(ctx, hub_id):
+    """Many fringes on one anchor: nck(2000, k) wraps for k >= 7.  With the hub
+    at the largest id and degree above 2048 the wedge core also runs its
+    high-degree endpoint kernel."""
+    g = graph("hub3000") if hub_id == 0 else hub_graph(3000, 2100, 8000, 4, hub_id)
     gid = ctx.upload(g)
     try:
         deg = g.degrees()
