@@ -239,21 +239,30 @@ def run_gpu(args, rank, world):
 
 
 def cpu_sample(g, mos, budget_s, threads):
-    """Time the oracle on a sample of each pattern's top-level work items
-    (every stride-th vertex), growing the sample until it takes ~budget_s."""
+    """Time the oracle (the reference's per-match formulas on the host cores)
+    on a hashed sample of each pattern's work items (the reference's worklist
+    entries), and extrapolate: t_full = t_scan + (t_sample - t_scan) * stride,
+    where t_scan is the cost of a pass that takes no item."""
     import oracle
     per = budget_s / len(mos)
     est, samples = 0.0, {}
     for name, mo in mos:
-        stride = 1 << 16
+        b = mo.to_bytes()
+        t0 = time.perf_counter()
+        oracle.count(g.nindex, g.nlist, b, stride=1 << 30, phase=1 << 29, threads=threads)
+        t_scan = time.perf_counter() - t0
+        stride = 1 << 24
         while True:
             t0 = time.perf_counter()
-            oracle.count(g.nindex, g.nlist, mo.to_bytes(), stride=stride, phase=stride // 2 + 1, threads=threads)
+            oracle.count(g.nindex, g.nlist, b, stride=stride, phase=stride // 3, threads=threads)
             t = time.perf_counter() - t0
-            if t >= per / 4 or stride == 1:
+            work = max(t - t_scan, 0.0)
+            if work >= per / 2 or stride == 1 or t >= per:
                 break
-            stride = max(1, stride // 4)
-        est += t * stride
+            # aim the next sample at ~per/2 seconds of work
+            grow = 16 if work <= 0 else min(16.0, max(2.0, (per / 2) / work))
+            stride = max(1, int(stride / grow))
+        est += t_scan + work * stride
         samples[name] = stride
     return est, samples
 

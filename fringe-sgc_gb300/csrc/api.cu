@@ -333,7 +333,6 @@ void fsgc_ctx_destroy(fsgc_ctx* c) {
   if (c->t1) cudaEventDestroy(c->t1);
   cudaFree(c->flush_buf);
   cudaFree(c->work.small);
-  cudaFree(c->work.pairs.ptr);
   cudaFree(c->work.tri.ptr);
   cudaFree(c->d_slots);
   cudaFreeHost(c->h_slots);

@@ -445,103 +445,127 @@ struct WedgeParams {
 };
 
 // Centre without fringes (wedgecore_specialized, src/fringeCount.cu:1409-1477).
-// One block per endpoint v (taken from a queue); for every centre u in N(v)
-// and every w < v in N(u) the pair (v, w) gets one more centre in a dense
-// per-block counter; then every touched pair is evaluated once with its
-// centre count C: C * wedge(v, w, C - 1).
-__global__ void __launch_bounds__(512) wedge_pair_kernel(GView g, WedgeParams p, unsigned* __restrict__ cnt_all,
-                                                         int* __restrict__ touched_all, int* __restrict__ queue,
-                                                         int dv_min, u64* __restrict__ slot) {
-  __shared__ int s_v, s_nt;
-  unsigned* cnt = cnt_all + (size_t)blockIdx.x * (size_t)g.n;
-  int* touched = touched_all + (size_t)blockIdx.x * (size_t)g.n;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  u64 acc = 0;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      s_v = atomicAdd(queue, 1);
-      s_nt = 0;
-    }
-    __syncthreads();
-    const int v = s_v;
-    if (v >= g.n) break;
-    const int dv = g.deg[v];
-    if (dv >= p.lim && dv >= dv_min) {
-      const int thres = max(p.lim, p.minsum - dv);
-      const long long vb = g.off[v];
-      for (int t = warp; t < dv; t += nwarp) {
-        const int u = g.adj[vb + t];
-        const long long ub = g.off[u];
-        const int du = g.deg[u];
-        for (int s = lane; s < du; s += 32) {
-          const int w = __ldg(g.adj + ub + s);
-          if (w >= v) break;
-          if (g.deg[w] >= thres) {
-            const unsigned old = atomicAdd(cnt + w, 1u);
-            if (old == 0) touched[atomicAdd(&s_nt, 1)] = w;
-          }
-        }
-      }
-      __syncthreads();
-      const int nt = s_nt;
-      const int* Nv = g.adj + vb;
-      for (int q = threadIdx.x; q < nt; q += blockDim.x) {
-        const int w = touched[q];
-        const unsigned C = cnt[w];
-        cnt[w] = 0;
-        const bool vw = bsearch_has(Nv, dv, w);
-        acc += (u64)C * wedge_formula(dv, g.deg[w], vw, p.f_v, p.f_vw, p.f_w, (int)C - 1);
-      }
-    }
-    __syncthreads();
-  }
-  block_sum_to(acc, slot);
-}
-
-// Same sum as wedge_pair_kernel, with the centre counts of endpoint v kept in
-// shared memory: the ids w < v are swept in chunks of kWCh; per chunk every
+// The reference evaluates wedge() once per (centre u, endpoints v > w); the
+// value depends only on the endpoints and their centre count C = |N(v) & N(w)|,
+// so here each endpoint pair is evaluated once and weighted by C: one block per
+// endpoint v (from a queue) counts, for every w < v, the centres u in N(v) with
+// w in N(u), with the counts kept in shared memory.  The ids w < v are swept in chunks of CH ids; per chunk every
 // centre u in N(v) contributes the segment of N(u) inside the chunk (a cursor
-// per centre walks each sorted list once), the segment lengths are prefix-
-// summed so that all threads share the chunk's elements evenly, counts go to
-// shared-memory counters, and only the touched counters are evaluated and
-// cleared.  Chunks no centre reaches are skipped.  Endpoints of degree above
-// kWDvMax are left to wedge_pair_kernel.
-constexpr int kWCh = 16384;
+// per centre walks each sorted list once; segment ends are found by galloping
+// from the cursor).  The segment lengths are prefix-summed and every warp takes
+// a contiguous range of the chunk's elements, following segment boundaries as
+// it goes.  Counts go to shared-memory counters; the counters are then scanned,
+// the non-zero ones compacted per warp so that every lane evaluates one pair,
+// and cleared.  Chunks no centre reaches are skipped.
+//
+// SMALL (deg v <= kWDvMax): two 16-bit counters per word (a centre count never
+// exceeds deg v < 2^16) and the per-centre cursors in shared memory.
+// BIG (hub endpoints): 32-bit counters, cursors in a per-block global array.
 constexpr int kWDvMax = 2048;
 constexpr int kWThreads = 1024;
+constexpr int kWBuf = 96;  // per-warp pair buffer (flushed 32 at a time)
 
-struct WedgeChunkSmem {
-  unsigned cnt[kWCh];
-  unsigned short touched[kWCh];
-  unsigned adjbits[kWCh / 32];
-  long long cur[kWDvMax];
-  long long lim[kWDvMax];
-  int pre[kWDvMax + 1];
-  int warp_tmp[32];
-  int nt;
+template <bool BIG>
+struct WedgeCfg {
+  static constexpr int CH = BIG ? 32768 : 65536;          // ids per chunk
+  static constexpr int WORDS = BIG ? CH : CH / 2;         // counter words
+};
+
+template <bool BIG>
+struct WedgeSmem {
+  unsigned cnt[WedgeCfg<BIG>::WORDS];
+  unsigned adjbits[WedgeCfg<BIG>::CH / 32];
+  long long cur[BIG ? 1 : kWDvMax];
+  long long lim[BIG ? 1 : kWDvMax];
+  int pre[BIG ? 1 : kWDvMax + 1];
+  int buf_o[32][kWBuf];
+  unsigned buf_c[32][kWBuf];
+  int warp_tmp[33];
   int v;
   int lo;
 };
 
-__global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, WedgeParams p, int* __restrict__ queue,
-                                                                   u64* __restrict__ slot) {
-  extern __shared__ unsigned char s_raw[];
-  WedgeChunkSmem& S = *reinterpret_cast<WedgeChunkSmem*>(s_raw);
+// first index i in [from, to) with a[i] >= x, searching outward from `from`
+__device__ __forceinline__ long long gallop_lb(const int* __restrict__ a, long long from, long long to, int x) {
+  if (from >= to || __ldg(a + from) >= x) return from;
+  long long p = from, step = 1;  // invariant: a[p] < x
+  while (p + step < to && __ldg(a + p + step) < x) {
+    p += step;
+    step <<= 1;
+  }
+  long long l = p + 1, r = min(p + step, to);  // answer in [l, r]
+  while (l < r) {
+    const long long m = (l + r) >> 1;
+    if (__ldg(a + m) < x) l = m + 1;
+    else r = m;
+  }
+  return l;
+}
+
+// block-wide exclusive scan of x[0..n) in place (x[n] = total); every thread calls
+template <bool BIG>
+__device__ void block_scan_inplace(int* x, int n, WedgeSmem<BIG>& S) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-  for (int i = tid; i < kWCh; i += blockDim.x) S.cnt[i] = 0;
-  for (int i = tid; i < kWCh / 32; i += blockDim.x) S.adjbits[i] = 0;
+  int carry = 0;
+  for (int base = 0; base < n; base += 2 * blockDim.x) {
+    const int i0 = base + 2 * tid, i1 = i0 + 1;
+    const int x0 = (i0 < n) ? x[i0] : 0, x1 = (i1 < n) ? x[i1] : 0;
+    const int sum = x0 + x1;
+    int inc = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) S.warp_tmp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+      const int wv = (lane < nwarp) ? S.warp_tmp[lane] : 0;
+      int wi = wv;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, wi, o);
+        if (lane >= o) wi += y;
+      }
+      if (lane < nwarp) S.warp_tmp[lane] = wi - wv;
+      if (lane == 31) S.warp_tmp[32] = wi;
+    }
+    __syncthreads();
+    const int ex = carry + S.warp_tmp[warp] + inc - sum;
+    if (i0 < n) x[i0] = ex;
+    if (i1 < n) x[i1] = ex + x0;
+    carry += S.warp_tmp[32];
+    __syncthreads();
+  }
+  if (tid == 0) x[n] = carry;
+}
+
+template <bool BIG>
+__global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, WedgeParams p, int* __restrict__ queue,
+                                                                   long long* __restrict__ gcur, int* __restrict__ gpre,
+                                                                   long long gstride, u64* __restrict__ slot) {
+  constexpr int CH = WedgeCfg<BIG>::CH;
+  constexpr int WORDS = WedgeCfg<BIG>::WORDS;
+  extern __shared__ unsigned char s_raw[];
+  WedgeSmem<BIG>& S = *reinterpret_cast<WedgeSmem<BIG>*>(s_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  long long* cur = BIG ? gcur + (size_t)blockIdx.x * 2 * gstride : S.cur;
+  long long* lim = BIG ? cur + gstride : S.lim;
+  int* pre = BIG ? gpre + (size_t)blockIdx.x * (gstride + 1) : S.pre;
+  for (int i = tid; i < WORDS; i += blockDim.x) S.cnt[i] = 0;
+  for (int i = tid; i < CH / 32; i += blockDim.x) S.adjbits[i] = 0;
   u64 acc = 0;
+  int* bo = S.buf_o[warp];
+  unsigned* bc = S.buf_c[warp];
   for (;;) {
     if (tid == 0) {
       S.v = atomicAdd(queue, 1);
-      S.nt = 0;
       S.lo = 0;
     }
     __syncthreads();
     const int v = S.v;
     if (v >= g.n) break;
     const int dv = g.deg[v];
-    if (dv < p.lim || dv > kWDvMax) {
+    if (dv < p.lim || (BIG ? dv <= kWDvMax : dv > kWDvMax)) {
       __syncthreads();
       continue;
     }
@@ -550,46 +574,18 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
     const int* Nv = g.adj + vb;
     for (int t = tid; t < dv; t += blockDim.x) {
       const int u = __ldg(Nv + t);
-      S.cur[t] = g.off[u];
-      S.lim[t] = g.off[u + 1];
+      cur[t] = g.off[u];
+      lim[t] = g.off[u + 1];
     }
     int cv = 0;  // cursor into N(v) for the adjacency marks
     __syncthreads();
     while (S.lo < v) {
       const int lo = S.lo;
-      const int hi = min(lo + kWCh, v);
-      // segment of each centre's list inside [lo, hi)
+      const int hi = min(lo + CH, v);
       for (int t = tid; t < dv; t += blockDim.x) {
-        const long long c = S.cur[t];
-        S.pre[t] = lower_bound_dev(g.adj + c, (int)(S.lim[t] - c), hi);
+        const long long c = cur[t];
+        pre[t] = (int)(gallop_lb(g.adj, c, lim[t], hi) - c);
       }
-      __syncthreads();
-      // exclusive scan of the segment lengths (dv <= kWDvMax <= 2 * blockDim)
-      {
-        int x0 = (2 * tid < dv) ? S.pre[2 * tid] : 0;
-        int x1 = (2 * tid + 1 < dv) ? S.pre[2 * tid + 1] : 0;
-        int sum = x0 + x1, inc = sum;
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(0xffffffffu, inc, o);
-          if (lane >= o) inc += y;
-        }
-        if (lane == 31) S.warp_tmp[warp] = inc;
-        __syncthreads();
-        if (warp == 0) {
-          int wv = (lane < nwarp) ? S.warp_tmp[lane] : 0, wi = wv;
-          for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += y;
-          }
-          if (lane < nwarp) S.warp_tmp[lane] = wi - wv;
-        }
-        __syncthreads();
-        const int ex = S.warp_tmp[warp] + inc - sum;
-        if (2 * tid < dv) S.pre[2 * tid] = ex;
-        if (2 * tid + 1 < dv) S.pre[2 * tid + 1] = ex + x0;
-        if (2 * tid + 1 == dv - 1 || 2 * tid == dv - 1) S.pre[dv] = ex + sum;
-      }
-      // adjacency marks for N(v) inside the chunk (chunks may have been skipped)
       const int cs = cv + lower_bound_dev(Nv + cv, dv - cv, lo);
       const int cend = cs + lower_bound_dev(Nv + cs, dv - cs, hi);
       for (int i = cs + tid; i < cend; i += blockDim.x) {
@@ -597,53 +593,104 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
         atomicOr(&S.adjbits[o >> 5], 1u << (o & 31));
       }
       __syncthreads();
-      const int L = S.pre[dv];
-      for (int e = tid; e < L; e += blockDim.x) {
-        // centre t owning element e: last t with pre[t] <= e
-        int a = 0, b = dv;
-        while (b - a > 1) {
-          const int mid = (a + b) >> 1;
-          if (S.pre[mid] <= e) a = mid;
-          else b = mid;
+      block_scan_inplace<BIG>(pre, dv, S);
+      __syncthreads();
+      // count: warp-contiguous ranges of the chunk's elements
+      {
+        const int L = pre[dv];
+        const int ws = (int)(((long long)L * warp) / nwarp), we = (int)(((long long)L * (warp + 1)) / nwarp);
+        if (ws < we) {
+          int a = 0, b = dv;  // last segment with pre <= ws
+          while (b - a > 1) {
+            const int mid = (a + b) >> 1;
+            if (pre[mid] <= ws) a = mid;
+            else b = mid;
+          }
+          for (int e0 = ws; e0 < we; e0 += 32) {
+            const int e = e0 + lane;
+            int al = a;
+            if (e < we) {
+              while (pre[al + 1] <= e) al++;
+              const int o = __ldg(g.adj + cur[al] + (e - pre[al])) - lo;
+              if (BIG) atomicAdd(&S.cnt[o], 1u);
+              else atomicAdd(&S.cnt[o >> 1], 1u << ((o & 1) << 4));
+            }
+            a = __shfl_sync(0xffffffffu, al, 31);
+          }
         }
-        const int w = __ldg(g.adj + S.cur[a] + (e - S.pre[a]));
-        const unsigned old = atomicAdd(&S.cnt[w - lo], 1u);
-        if (old == 0) S.touched[atomicAdd(&S.nt, 1)] = (unsigned short)(w - lo);
       }
       __syncthreads();
-      const int nt = S.nt;
-      for (int q = tid; q < nt; q += blockDim.x) {
-        const int o = S.touched[q];
-        const unsigned C = S.cnt[o];
-        S.cnt[o] = 0;
-        const int w = lo + o;
-        const int dw = g.deg[w];
-        if (dw >= thres) {
-          const bool vw = (S.adjbits[o >> 5] >> (o & 31)) & 1u;
-          acc += (u64)C * wedge_formula(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1);
+      // evaluate: warp ranges of counter words, non-zero counters compacted
+      {
+        const int nw = BIG ? (hi - lo) : ((hi - lo + 1) >> 1);
+        const int ws = (int)(((long long)nw * warp) / nwarp), we = (int)(((long long)nw * (warp + 1)) / nwarp);
+        int nb = 0;
+        auto flush = [&](int count) {
+          if (lane < count) {
+            const int o = bo[lane];
+            const unsigned C = bc[lane];
+            const int w = lo + o;
+            const int dw = g.deg[w];
+            if (dw >= thres) {
+              const bool vw = (S.adjbits[o >> 5] >> (o & 31)) & 1u;
+              acc += (u64)C * wedge_formula(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1);
+            }
+          }
+        };
+        for (int i0 = ws; i0 < we; i0 += 32) {
+          const int i = i0 + lane;
+          unsigned word = 0;
+          if (i < we) {
+            word = S.cnt[i];
+            if (word) S.cnt[i] = 0;
+          }
+          constexpr int PER = BIG ? 1 : 2;
+#pragma unroll
+          for (int h = 0; h < PER; h++) {
+            const unsigned C = BIG ? word : ((word >> (16 * h)) & 0xffffu);
+            const bool has = C != 0;
+            const unsigned bal = __ballot_sync(0xffffffffu, has);
+            if (has) {
+              const int q = nb + __popc(bal & lt);
+              bo[q] = BIG ? i : 2 * i + h;
+              bc[q] = C;
+            }
+            nb += __popc(bal);
+          }
+          __syncwarp();
+          while (nb >= 32) {
+            flush(32);
+            __syncwarp();
+            const int rest = nb - 32;
+            for (int q = lane; q < rest; q += 32) {
+              const int src = 32 + q;
+              const int oo = bo[src];  // src >= 32 > q: no lane reads what another writes
+              const unsigned cc = bc[src];
+              bo[q] = oo;
+              bc[q] = cc;
+            }
+            __syncwarp();
+            nb = rest;
+          }
         }
+        flush(nb);
+        __syncwarp();
       }
-      __syncthreads();  // adjbits and pre are still read above
-      for (int i = tid; i < kWCh / 32; i += blockDim.x) S.adjbits[i] = 0;
       // advance the cursors and find the next id any centre still reaches
       int nxt = 0x7fffffff;
       for (int t = tid; t < dv; t += blockDim.x) {
-        const long long c = S.cur[t] + (S.pre[t + 1] - S.pre[t]);
-        S.cur[t] = c;
-        if (c < S.lim[t]) nxt = min(nxt, __ldg(g.adj + c));
+        const long long c = cur[t] + (pre[t + 1] - pre[t]);
+        cur[t] = c;
+        if (c < lim[t]) nxt = min(nxt, __ldg(g.adj + c));
       }
       nxt = __reduce_min_sync(0xffffffffu, nxt);
       cv = cend;
-      __syncthreads();
-      if (tid == 0) {
-        S.nt = 0;
-        S.lo = v;
-      }
-      __syncthreads();
+      if (tid == 0) S.lo = v;
+      __syncthreads();  // adjbits, pre and S.lo are free again
+      for (int i = tid; i < (CH >> 5); i += blockDim.x) S.adjbits[i] = 0;
       if (lane == 0) atomicMin(&S.lo, max(hi, nxt));
       __syncthreads();
     }
-    __syncthreads();
   }
   block_sum_to(acc, slot);
 }
@@ -990,34 +1037,6 @@ int ensure_plain_scratch(Scratch& sc, size_t need, cudaStream_t s) {
   return FSGC_OK;
 }
 
-// Pair-counter scratch for the wedge core: `blocks` rows of n counters plus
-// `blocks` rows of n touched-list entries.  Counters are zero whenever no
-// kernel is running (each launch clears what it touched), so they are only
-// cleared when the row layout changes.
-int ensure_pair_scratch(Scratch& sc, int n, int blocks, cudaStream_t s) {
-  const size_t need = (size_t)blocks * (size_t)n * (sizeof(unsigned) + sizeof(int));
-  if (sc.bytes < need) {
-    if (sc.ptr) {
-      cudaStreamSynchronize(s);
-      cudaFree(sc.ptr);
-      sc.ptr = nullptr;
-      sc.bytes = 0;
-    }
-    if (cudaMalloc(&sc.ptr, need) != cudaSuccess) {
-      cudaGetLastError();
-      return FSGC_ENOMEM;
-    }
-    sc.bytes = need;
-    sc.layout_n = -1;
-  }
-  if (sc.layout_n != n || sc.layout_rows != blocks) {
-    if (cudaMemsetAsync(sc.ptr, 0, (size_t)blocks * (size_t)n * sizeof(unsigned), s) != cudaSuccess) return FSGC_ECUDA;
-    sc.layout_n = n;
-    sc.layout_rows = blocks;
-  }
-  return FSGC_OK;
-}
-
 }  // namespace
 
 int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work) {
@@ -1089,28 +1108,29 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
     const int lim = std::min(min_v, min_w);
     if (f[IUVW] == 0 && f[IUV] == 0 && f[IUW] == 0 && f[IU] == 0) {
       WedgeParams wp{f[IV], f[IVW], f[IW], lim, min_v + min_w};
+      int* q1 = reinterpret_cast<int*>(work.small + 7);
+      int* q2 = reinterpret_cast<int*>(work.small + 8);
+      cudaMemsetAsync(q1, 0, 2 * sizeof(u64), s);
+      const int blocks = sm_count();
       {
-        int* q1 = reinterpret_cast<int*>(work.small + 7);
-        cudaMemsetAsync(q1, 0, sizeof(int), s);
-        const size_t smem = sizeof(WedgeChunkSmem);
-        cudaFuncSetAttribute(wedge_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        wedge_chunk_kernel<<<sm_count(), kWThreads, smem, s>>>(gv, wp, q1, job.d_slot);
+        const size_t smem = sizeof(WedgeSmem<false>);
+        cudaFuncSetAttribute(wedge_chunk_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        wedge_chunk_kernel<false><<<blocks, kWThreads, smem, s>>>(gv, wp, q1, nullptr, nullptr, 0, job.d_slot);
         *launches += 1;
       }
-      if (G.maxdeg <= kWDvMax) return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
-      // dense per-block pair counters + touched lists, bounded to 16 GiB
-      const size_t per_block = (size_t)G.n * (sizeof(unsigned) + sizeof(int));
-      int blocks = sm_count() * 2;
-      const size_t budget = (size_t)16 << 30;
-      blocks = (int)std::max<size_t>(1, std::min<size_t>((size_t)blocks, budget / std::max<size_t>(1, per_block)));
-      st = ensure_pair_scratch(work.pairs, G.n, blocks, s);
-      if (st != FSGC_OK) return st;
-      int* queue = reinterpret_cast<int*>(work.small + 4);
-      cudaMemsetAsync(queue, 0, sizeof(int), s);
-      unsigned* cnt = reinterpret_cast<unsigned*>(work.pairs.ptr);
-      int* touched = reinterpret_cast<int*>(cnt + (size_t)blocks * G.n);
-      wedge_pair_kernel<<<blocks, 512, 0, s>>>(gv, wp, cnt, touched, queue, kWDvMax + 1, job.d_slot);
-      *launches += 1;
+      if (G.maxdeg > kWDvMax) {
+        // hub endpoints: cursors (2 x int64) and segment offsets (int32) per block
+        const long long gs = G.maxdeg;
+        const size_t need = (size_t)blocks * ((size_t)2 * gs * sizeof(long long) + (size_t)(gs + 1) * sizeof(int));
+        st = ensure_plain_scratch(work.tri, std::max(need, work.tri.bytes), s);
+        if (st != FSGC_OK) return st;
+        long long* gcur = reinterpret_cast<long long*>(work.tri.ptr);
+        int* gpre = reinterpret_cast<int*>(gcur + (size_t)blocks * 2 * gs);
+        const size_t smem = sizeof(WedgeSmem<true>);
+        cudaFuncSetAttribute(wedge_chunk_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        wedge_chunk_kernel<true><<<blocks, kWThreads, smem, s>>>(gv, wp, q2, gcur, gpre, gs, job.d_slot);
+        *launches += 1;
+      }
       return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
     }
     GWedgeParams gp;

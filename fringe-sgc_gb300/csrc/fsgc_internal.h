@@ -65,11 +65,11 @@ struct Scratch {
   int layout_n = -1, layout_rows = -1;
 };
 
-// Per-context device work areas: a few u64 counters/queues and the wedge-core
-// pair counters.
+// Per-context device work areas: a few u64 counters/queues (kernel work
+// queues, loader results) and a growable scratch arena (triangle-core bitmaps,
+// wedge-core hub cursors).
 struct DevWork {
   u64* small = nullptr;  // 32 u64
-  Scratch pairs;
   Scratch tri;
 };
 

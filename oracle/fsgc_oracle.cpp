@@ -170,11 +170,22 @@ static int rotations3(const int f[8], int fr[6][8], bool wedge) {
   return p;
 }
 
-// Sampling: top-level work items (the vertex that owns a worklist entry) are
-// processed only when v % stride == phase.  stride 1 processes everything.
+// Sampling for the CPU baseline: the reference's work items -- vertices for
+// the vertex core, worklist entries (u, v) for the other cores -- are processed
+// only when a hash of the item falls in residue `phase` modulo `stride`.
+// stride 1 processes everything.
 struct Sample {
   int stride = 1, phase = 0;
-  bool take(int v) const { return stride <= 1 || (v % stride) == phase; }
+  static u64 mix(u64 x) {
+    x += 0x9e3779b97f4a7c15ULL;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
+    return x ^ (x >> 31);
+  }
+  bool take(int v) const { return stride <= 1 || (int)(mix((u64)(unsigned)v) % (u64)stride) == phase; }
+  bool take(int u, int v) const {
+    return stride <= 1 || (int)(mix(((u64)(unsigned)u << 32) | (unsigned)v) % (u64)stride) == phase;
+  }
 };
 
 // ---------------------------------------------------------------- vertex core
@@ -219,13 +230,13 @@ static u64 edge_core(const MO& mo, const Graph& g, const Sample& s) {
   u64 tot = 0;
 #pragma omp parallel for reduction(+ : tot) schedule(dynamic, 64)
   for (int u = 0; u < g.n; u++) {
-    if (!s.take(u)) continue;
     const int du = g.deg(u);
     if (du <= lim1) continue;
     const u64 cu = special ? nck(du - 2, f_v) : 0;
     for (const int* p = g.beg(u); p < g.end(u) && *p < u; p++) {
       const int v = *p, dv = g.deg(v);
       if (!(dv > lim1 && du + dv > lim2)) continue;
+      if (!s.take(u, v)) continue;
       if (special) {
         // triangles w < v < u
         const u64 c12 = cu + nck(dv - 2, f_v);
@@ -302,10 +313,10 @@ static u64 wedge_core(const MO& mo, const Graph& g, const Sample& s) {
     const int fv = f[IV], fvw = f[IVW], fw = f[IW];
 #pragma omp parallel for reduction(+ : tot) schedule(dynamic, 16)
     for (int u = 0; u < g.n; u++) {
-      if (!s.take(u) || g.deg(u) < 2) continue;
+      if (g.deg(u) < 2) continue;
       for (const int* pv = g.beg(u); pv < g.end(u); pv++) {
         const int v = *pv, dv = g.deg(v);
-        if (dv < lim) continue;
+        if (dv < lim || !s.take(u, v)) continue;
         const int thres = std::max(lim, min_v + min_w - dv);
         for (const int* pw = g.beg(u); pw < g.end(u) && *pw < v; pw++) {
           const int w = *pw, dw = g.deg(w);
@@ -321,13 +332,12 @@ static u64 wedge_core(const MO& mo, const Graph& g, const Sample& s) {
   const int rot = rotations3(f, fr, true);
 #pragma omp parallel for reduction(+ : tot) schedule(dynamic, 16)
   for (int u = 0; u < g.n; u++) {
-    if (!s.take(u)) continue;
     const int du = g.deg(u);
     if (du < sum1) continue;
     const int th1u = std::max(sum1, sum2 - du);
     for (const int* pv = g.beg(u); pv < g.end(u); pv++) {
       const int v = *pv, dv = g.deg(v);
-      if (dv < th1u) continue;  // init_wl_wedge
+      if (dv < th1u || !s.take(u, v)) continue;  // init_wl_wedge
       const int p12 = common2(g, u, v);
       const bool cond = (du >= min_u) && (dv >= lim);
       const int thres1 = std::max(lim, sum2 - dv);
@@ -396,7 +406,6 @@ static u64 triangle_core(const MO& mo, const Graph& g, const Sample& s) {
   u64 tot = 0;
 #pragma omp parallel for reduction(+ : tot) schedule(dynamic, 16)
   for (int u = 0; u < g.n; u++) {
-    if (!s.take(u)) continue;
     const int du = g.deg(u);
     if (du < sum1) continue;
     const int th1 = std::max(sum1, sum2 - du);
@@ -405,6 +414,7 @@ static u64 triangle_core(const MO& mo, const Graph& g, const Sample& s) {
       const int v = *pv, dv = g.deg(v);
       const long long kv = ord.key(v);
       if (!(kv < ku) || dv < th1) continue;  // init_wl_triangle: v before u
+      if (!s.take(u, v)) continue;
       // w in N(u) & N(v) with w before v
       std::vector<int> ws;
       for (const int* pw = g.beg(u); pw < g.end(u); pw++)
@@ -572,13 +582,13 @@ static u64 general_core(const MO& mo, const Graph& g, const Sample& s) {
   u64 tot = 0;
 #pragma omp parallel for reduction(+ : tot) schedule(dynamic, 4)
   for (int u = 0; u < g.n; u++) {
-    if (!s.take(u) || g.deg(u) < mo.startdeg) continue;
+    if (g.deg(u) < mo.startdeg) continue;
     GenCtx c;
     c.mo = &mo; c.g = &g; c.k = k; c.anchors = anchors;
     c.nonanchors = anchors ^ ((1 << k) - 1);
     for (const int* p = g.beg(u); p < g.end(u); p++) {
       const int v = *p;
-      if (g.deg(v) < mo.destdeg[0]) continue;  // init_wl_general
+      if (g.deg(v) < mo.destdeg[0] || !s.take(u, v)) continue;  // init_wl_general
       c.stack[0] = u;
       c.stack[1] = v;
       tot += gen_dfs(c, 1);
