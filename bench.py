@@ -297,8 +297,8 @@ def main():
                 "config": {"workload": "RMAT scale 22, edge factor 16, (a,b,c,d)=(.57,.19,.19,.05), 8 patterns",
                            "patterns": list(WORKLOAD)},
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                                 "sample": "every stride-th top-level vertex per pattern, strides " +
-                                           json.dumps(samples) + ", time x stride"},
+                                 "sample": "hashed 1/stride of each pattern's worklist items, strides " +
+                                           json.dumps(samples) + "; t_scan + (t - t_scan) x stride"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -332,7 +332,8 @@ def main():
     if world == 1 and args.cpu_budget > 0:
         est, samples = cpu_sample(g, mos, args.cpu_budget, os.cpu_count() or 1)
         cpu = {"value": len(mos) / est, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": "oracle on every stride-th top-level vertex per pattern, strides " + json.dumps(samples)}
+               "sample": "oracle on a hashed 1/stride of each pattern's worklist items, strides " +
+                         json.dumps(samples) + "; t_scan + (t - t_scan) x stride"}
     h2d = 8 * (g.n + 1) + 4 * g.m
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

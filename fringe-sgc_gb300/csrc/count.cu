@@ -474,6 +474,7 @@ struct WedgeCfg {
 template <bool BIG>
 struct WedgeSmem {
   unsigned cnt[WedgeCfg<BIG>::WORDS];
+  unsigned touched[WedgeCfg<BIG>::WORDS / 32];  // counter words that became non-zero
   unsigned adjbits[WedgeCfg<BIG>::CH / 32];
   long long cur[BIG ? 1 : kWDvMax];
   long long lim[BIG ? 1 : kWDvMax];
@@ -552,6 +553,7 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
   long long* lim = BIG ? cur + gstride : S.lim;
   int* pre = BIG ? gpre + (size_t)blockIdx.x * (gstride + 1) : S.pre;
   for (int i = tid; i < WORDS; i += blockDim.x) S.cnt[i] = 0;
+  for (int i = tid; i < WORDS / 32; i += blockDim.x) S.touched[i] = 0;
   for (int i = tid; i < CH / 32; i += blockDim.x) S.adjbits[i] = 0;
   u64 acc = 0;
   int* bo = S.buf_o[warp];
@@ -612,18 +614,22 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
             if (e < we) {
               while (pre[al + 1] <= e) al++;
               const int o = __ldg(g.adj + cur[al] + (e - pre[al])) - lo;
-              if (BIG) atomicAdd(&S.cnt[o], 1u);
-              else atomicAdd(&S.cnt[o >> 1], 1u << ((o & 1) << 4));
+              const int wd = BIG ? o : (o >> 1);
+              const unsigned old = atomicAdd(&S.cnt[wd], BIG ? 1u : (1u << ((o & 1) << 4)));
+              if (old == 0) atomicOr(&S.touched[wd >> 5], 1u << (wd & 31));
             }
             a = __shfl_sync(0xffffffffu, al, 31);
           }
         }
       }
       __syncthreads();
-      // evaluate: warp ranges of counter words, non-zero counters compacted
+      // evaluate: warps take ranges of the touched-word bitmap; each lane walks
+      // the set bits of one bitmap word; non-zero counters are compacted so
+      // that every lane evaluates one pair per flush
       {
         const int nw = BIG ? (hi - lo) : ((hi - lo + 1) >> 1);
-        const int ws = (int)(((long long)nw * warp) / nwarp), we = (int)(((long long)nw * (warp + 1)) / nwarp);
+        const int nt = (nw + 31) >> 5;
+        const int ws = (int)(((long long)nt * warp) / nwarp), we = (int)(((long long)nt * (warp + 1)) / nwarp);
         int nb = 0;
         auto flush = [&](int count) {
           if (lane < count) {
@@ -637,40 +643,50 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
             }
           }
         };
-        for (int i0 = ws; i0 < we; i0 += 32) {
-          const int i = i0 + lane;
-          unsigned word = 0;
-          if (i < we) {
-            word = S.cnt[i];
-            if (word) S.cnt[i] = 0;
+        for (int t0 = ws; t0 < we; t0 += 32) {
+          const int t = t0 + lane;
+          unsigned mask = 0;
+          if (t < we) {
+            mask = S.touched[t];
+            if (mask) S.touched[t] = 0;
           }
-          constexpr int PER = BIG ? 1 : 2;
+          while (__any_sync(0xffffffffu, mask != 0)) {
+            unsigned word = 0;
+            int wd = 0;
+            if (mask) {
+              const int b = __ffs(mask) - 1;
+              mask &= mask - 1;
+              wd = (t << 5) + b;
+              word = S.cnt[wd];
+              S.cnt[wd] = 0;
+            }
+            constexpr int PER = BIG ? 1 : 2;
 #pragma unroll
-          for (int h = 0; h < PER; h++) {
-            const unsigned C = BIG ? word : ((word >> (16 * h)) & 0xffffu);
-            const bool has = C != 0;
-            const unsigned bal = __ballot_sync(0xffffffffu, has);
-            if (has) {
-              const int q = nb + __popc(bal & lt);
-              bo[q] = BIG ? i : 2 * i + h;
-              bc[q] = C;
-            }
-            nb += __popc(bal);
-          }
-          __syncwarp();
-          while (nb >= 32) {
-            flush(32);
-            __syncwarp();
-            const int rest = nb - 32;
-            for (int q = lane; q < rest; q += 32) {
-              const int src = 32 + q;
-              const int oo = bo[src];  // src >= 32 > q: no lane reads what another writes
-              const unsigned cc = bc[src];
-              bo[q] = oo;
-              bc[q] = cc;
+            for (int h = 0; h < PER; h++) {
+              const unsigned C = BIG ? word : ((word >> (16 * h)) & 0xffffu);
+              const bool has = C != 0;
+              const unsigned bal = __ballot_sync(0xffffffffu, has);
+              if (has) {
+                const int q = nb + __popc(bal & lt);
+                bo[q] = BIG ? wd : 2 * wd + h;
+                bc[q] = C;
+              }
+              nb += __popc(bal);
             }
             __syncwarp();
-            nb = rest;
+            while (nb >= 32) {
+              flush(32);
+              __syncwarp();
+              const int rest = nb - 32;
+              for (int q = lane; q < rest; q += 32) {
+                const int oo = bo[32 + q];  // 32 + q > q: no lane reads what another writes
+                const unsigned cc = bc[32 + q];
+                bo[q] = oo;
+                bc[q] = cc;
+              }
+              __syncwarp();
+              nb = rest;
+            }
           }
         }
         flush(nb);
