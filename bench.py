@@ -115,16 +115,16 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def workload_graph():
+def workload_graph(scale=None):
     import fsgc
     t = time.time()
-    g = fsgc.gen_rmat(RMAT["scale"], RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], RMAT["seed"])
+    g = fsgc.gen_rmat(scale or RMAT["scale"], RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], RMAT["seed"])
     return g, time.time() - t
 
 
-def matching_orders():
+def matching_orders(names=None):
     import fsgc
-    return [(name, fsgc.preprocess(n, e)) for name, (n, e) in WORKLOAD.items()]
+    return [(name, fsgc.preprocess(n, e)) for name, (n, e) in WORKLOAD.items() if not names or name in names]
 
 
 def wedge_bytes(g):
@@ -151,8 +151,8 @@ def run_gpu(args, rank, world):
     import fsgc
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = fsgc.Context(dev)
-    g, gen_s = workload_graph()
-    mos = matching_orders()
+    g, gen_s = workload_graph(args.scale)
+    mos = matching_orders(args.patterns)
     tasks_of = lambda gid: [(gid, mo) for _, mo in mos]  # noqa: E731
     # raw CSR resident in HBM for the device-resident measurement
     import ctypes as C
@@ -274,15 +274,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fsgc", choices=["fsgc", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
+    ap.add_argument("--scale", type=int, default=None, help="RMAT scale (profiling runs; default 22)")
+    ap.add_argument("--patterns", default=None, help="comma-separated subset of the patterns (profiling runs)")
     args = ap.parse_args()
+    if args.patterns:
+        args.patterns = args.patterns.split(",")
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     threads = os.cpu_count() or 1
     if args.impl == "reference":
         if rank != 0:
             return
-        g, _ = workload_graph()
-        mos = matching_orders()
+        g, _ = workload_graph(args.scale)
+        mos = matching_orders(args.patterns)
         for _ in range(args.warmup):
             cpu_sample(g, mos, args.cpu_budget / 4, threads)
         ests = []
