@@ -1235,4 +1235,26 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }
 
+// Launchers for callers that bring their own device memory (noalloc.cu): the
+// wedge-core pair kernels on a view whose deg[] the caller filled.
+int launch_wedge_small(const GView& gv, int f_v, int f_vw, int f_w, int lim, int minsum, int* queue, u64* slot,
+                       cudaStream_t s) {
+  WedgeParams wp{f_v, f_vw, f_w, lim, minsum};
+  const size_t smem = sizeof(WedgeSmem<false>);
+  cudaFuncSetAttribute(wedge_chunk_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  wedge_chunk_kernel<false><<<sm_count(), kWThreads, smem, s>>>(gv, wp, queue, nullptr, nullptr, 0, slot);
+  return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+
+int launch_wedge_big(const GView& gv, int f_v, int f_vw, int f_w, int lim, int minsum, int* queue, long long* gcur,
+                     int* gpre, long long gstride, int blocks, u64* slot, cudaStream_t s) {
+  WedgeParams wp{f_v, f_vw, f_w, lim, minsum};
+  const size_t smem = sizeof(WedgeSmem<true>);
+  cudaFuncSetAttribute(wedge_chunk_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  wedge_chunk_kernel<true><<<blocks, kWThreads, smem, s>>>(gv, wp, queue, gcur, gpre, gstride, slot);
+  return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+
+int wedge_small_max_degree() { return kWDvMax; }
+
 }  // namespace fsgc

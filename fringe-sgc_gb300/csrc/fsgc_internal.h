@@ -91,6 +91,14 @@ struct CountJob {
   bool host_only;
 };
 
+// Launchers over caller-provided device memory (used by noalloc.cu).
+int launch_degrees(int n, const long long* off, int* deg, int* maxdeg, cudaStream_t s);
+int launch_wedge_small(const GView& gv, int f_v, int f_vw, int f_w, int lim, int minsum, int* queue, u64* slot,
+                       cudaStream_t s);
+int launch_wedge_big(const GView& gv, int f_v, int f_vw, int f_w, int lim, int minsum, int* queue, long long* gcur,
+                     int* gpre, long long gstride, int blocks, u64* slot, cudaStream_t s);
+int wedge_small_max_degree();
+
 // Enqueue the kernels that add the raw total of `mo` on `g` into *d_slot.
 int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work);
 

@@ -257,6 +257,12 @@ static int grid_for(long long work, int tpb, int per_sm) {
     if (e__ != cudaSuccess) return FSGC_ECUDA;    \
   } while (0)
 
+// Degrees and the maximum degree into caller-provided device memory.
+int launch_degrees(int n, const long long* off, int* deg, int* maxdeg, cudaStream_t s) {
+  degree_kernel<<<grid_for(n, kTPB, 8), kTPB, 0, s>>>(n, off, deg, maxdeg);
+  return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+
 // Degrees and the maximum degree; run when a graph becomes resident.
 int graph_degrees(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_u64) {
   int* d_max = reinterpret_cast<int*>(d_u64);

@@ -100,6 +100,8 @@ def lib():
             "fsgc_ctx_timer_stop": (I, [P, C.POINTER(C.c_double)]),
             "fsgc_ctx_flush_l2": (I, [P, C.c_size_t]),
             "fsgc_ctx_synchronize": (I, [P]),
+            "fsgc_count_wedge_noalloc": (I, [I, I64, P, P, C.POINTER(MatchingOrder), P, C.POINTER(Result),
+                                             C.c_char_p, I]),
             "fsgc_nck_host": (C.c_ulonglong, [I, I]),
             "fsgc_div_small_host": (C.c_ulonglong, [C.c_ulonglong, C.c_uint]),
         }
@@ -223,6 +225,17 @@ def validate(g):
 
 
 # ----------------------------------------------------------------- device
+def count_wedge_noalloc(n, m, d_nindex, d_nlist, mo, stream=None):
+    """Allocation-free wedge-core count over a caller-owned device CSR
+    (fsgc_count_wedge_noalloc); returns a Result."""
+    r = Result()
+    err = C.create_string_buffer(256)
+    st = lib().fsgc_count_wedge_noalloc(n, m, d_nindex, d_nlist, C.byref(mo), stream, C.byref(r), err, 256)
+    if st != 0:
+        raise FsgcError(f"count_wedge_noalloc failed with status {st}: {err.value.decode()}")
+    return r
+
+
 class Context:
     def __init__(self, device=0):
         self.ptr = C.c_void_p()

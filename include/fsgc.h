@@ -166,6 +166,23 @@ typedef struct fsgc_task {
 } fsgc_task;
 int fsgc_count_batch(fsgc_ctx* ctx, const fsgc_task* tasks, int ntasks, fsgc_result* results);
 
+/* ---- allocation-free count (no counterpart in the reference) ----
+ * For callers that cannot allocate device memory when they count -- code
+ * running where a host framework forbids cudaMalloc after start-up, or inside
+ * another library's memory pool.  The caller passes its own device CSR
+ * (d_nindex[n+1] int64, d_nlist[m] int32 on the current device) and a stream
+ * (NULL = default stream); the count of a wedge-core pattern whose centre
+ * carries no fringes is written to *out.  Every intermediate lives in one fixed
+ * 64 MiB device array inside the library (held by each GPU that loads it until
+ * the process exits); graphs that do not fit (about 16M vertices, fewer when
+ * hub endpoints are large) and other pattern shapes return FSGC_EUNSUPPORTED.
+ * The first call on a device looks up that array's device address and loads a
+ * constant table; make that first call before any stream capture.  All calls
+ * share the array, so calls that overlap on the GPU race: serialise them. */
+int fsgc_count_wedge_noalloc(int n, int64_t m, const int64_t* d_nindex, const int32_t* d_nlist,
+                             const fsgc_matching_order* mo, void* stream, fsgc_result* out, char* errbuf,
+                             int errlen);
+
 #ifdef __cplusplus
 }
 #endif
