@@ -35,6 +35,7 @@ struct fsgc_ctx {
   std::vector<cudaEvent_t> events;
   std::map<std::string, u64> aut_cache;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
+  int exact_placements = 0;
   void* flush_buf = nullptr;
   size_t flush_bytes = 0;
 };
@@ -169,7 +170,8 @@ bool mo_valid(const fsgc_matching_order& mo) {
 // The divisor for cores of 3+ vertices: the pattern counted in itself with the
 // same kernels.  The reference stores it in an int (src/fringeCount.cu:2213).
 int automorphisms(fsgc_ctx* c, const fsgc_matching_order& mo, u64* out) {
-  const std::string key(reinterpret_cast<const char*>(&mo), sizeof(mo));
+  std::string key(reinterpret_cast<const char*>(&mo), sizeof(mo));
+  key.push_back(c->exact_placements ? 'x' : 'r');
   auto it = c->aut_cache.find(key);
   if (it != c->aut_cache.end()) {
     *out = it->second;
@@ -185,7 +187,7 @@ int automorphisms(fsgc_ctx* c, const fsgc_matching_order& mo, u64* out) {
   st = ensure_slots(c, 1);
   if (st != FSGC_OK) { free_graph(pg); return st; }
   cudaMemsetAsync(c->d_slots, 0, sizeof(u64), c->stream);
-  fsgc::CountJob job{&mo, pg, c->d_slots, 0, 0, false};
+  fsgc::CountJob job{&mo, pg, c->d_slots, 0, 0, false, c->exact_placements};
   st = fsgc::enqueue_count(job, c->stream, &c->launches, c->work);
   u64 raw = 0;
   if (st == FSGC_OK) {
@@ -250,7 +252,7 @@ int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
   for (int t = 0; t < nt; t++) {
     const fsgc_matching_order& mo = tasks[t].mo;
     DevGraph* g = find_graph(c, tasks[t].gid);
-    jobs[t] = fsgc::CountJob{&tasks[t].mo, g, c->d_slots + t, 0, 0, false};
+    jobs[t] = fsgc::CountJob{&tasks[t].mo, g, c->d_slots + t, 0, 0, false, c->exact_placements};
     if (pattern_too_large(mo, *g)) {
       jobs[t].host_only = true;
       jobs[t].host_value = 0;
@@ -384,6 +386,13 @@ int fsgc_ctx_flush_l2(fsgc_ctx* c, size_t bytes) {
   static unsigned char pattern = 0;
   pattern++;
   CK(cudaMemsetAsync(c->flush_buf, pattern, bytes, c->stream), "flush");
+  return FSGC_OK;
+}
+
+int fsgc_ctx_set_exact_placements(fsgc_ctx* c, int on) {
+  if (!c) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->exact_placements = on ? 1 : 0;
   return FSGC_OK;
 }
 

@@ -821,6 +821,9 @@ struct GenParams {
   uint8_t slot_set[kMaxSlots];  // anchor set index of each step
   uint8_t slot_top[kMaxSlots];  // 1 if the step takes all remaining fringes
   uint8_t fcnt[63];
+  uint8_t anch[63];
+  int nsets;
+  int exact;  // 1: exact placement sum; 0: the reference's functionX
 };
 
 // Placement sum (functionX, src/fringeCount.cu:408-486) over the precomputed
@@ -859,6 +862,61 @@ __device__ u64 placement_sum(const GenParams& p, int* venn) {
     rem_[ns] = p.slot_top[s] ? (int)p.fcnt[p.slot_set[ns]] : rem_[s] - a_[s];
     a_[ns] = p.slot_top[ns] ? rem_[ns] : min(venn[p.slot_idx[ns]], rem_[ns]);
     s = ns;
+  }
+  return sum;
+}
+
+// functionX with the reference's own control flow (src/fringeCount.cu:408-486),
+// the default: a flat depth-first walk that saves (a, prod, region,
+// venn[region], fr[set]) per level and, when it backs up, restores only the
+// level it returns to.  A region changed by the step it abandons keeps that
+// change, so later alternatives can see it reduced; for anchor sets with two
+// or more fringes the sum then differs from placement_sum (the exact count),
+// and the reference's counts are these sums.
+__device__ u64 placement_sum_reference(const GenParams& p, int* venn) {
+  int savea[kMaxSlots], savevenn[kMaxSlots];
+  u64 saveprod[kMaxSlots];
+  uint8_t saveidx[kMaxSlots], savefr[kMaxSlots];
+  uint8_t fr[64];
+  for (int i = 0; i < 64; i++) fr[i] = 0;
+  for (int i = 0; i < p.nsets; i++) fr[p.anch[i]] = p.fcnt[i];
+  const int top = p.anchors, non = p.nonanchors;
+  int asi = p.nsets - 1;
+  u64 sum = 0, prod = 1;
+  int level = 0;
+  int anch = p.anch[asi];
+  int idx = anch;
+  int a = min(venn[idx], (int)fr[anch]);
+  for (;;) {
+    savea[level] = a; saveprod[level] = prod; saveidx[level] = (uint8_t)idx;
+    savevenn[level] = venn[idx]; savefr[level] = fr[anch];
+    if (a < 0) {
+      prod = 0;
+    } else if (idx == top) {
+      prod *= nck(venn[idx], fr[anch]);
+      venn[idx] -= fr[anch];
+      fr[anch] = 0;
+      if (asi == 0) { sum += prod; prod = 0; }
+    } else {
+      prod *= nck(venn[idx], a);
+      venn[idx] -= a;
+      fr[anch] = (uint8_t)(fr[anch] - a);
+    }
+    if (prod == 0) {
+      level--;
+      if (level < 0) break;
+      a = savea[level] - 1;
+      prod = saveprod[level];
+      idx = saveidx[level];
+      if (idx == top) { asi++; anch = p.anch[asi]; }
+      venn[idx] = savevenn[level];
+      fr[anch] = savefr[level];
+    } else {
+      level++;
+      if (idx == top) { asi--; anch = p.anch[asi]; idx = anch; }
+      else idx = (((idx | non) + 1) | anch) & ~non;
+      a = (idx == top) ? 0 : min(venn[idx], (int)fr[anch]);
+    }
   }
   return sum;
 }
@@ -958,7 +1016,7 @@ __device__ u64 gen_level(const GView& g, const GenParams& p, GenWarp& w) {
         venn_general(g, p, w.stack, w.venn[who]);
       }
       __syncwarp();
-      if (ok) acc += placement_sum(p, w.venn[lane]);
+      if (ok) acc += p.exact ? placement_sum(p, w.venn[lane]) : placement_sum_reference(p, w.venn[lane]);
       __syncwarp();
     } else {
       while (bal) {
@@ -1209,6 +1267,9 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
   gp->startdeg = mo.startdeg;
   for (int i = 0; i < 5; i++) { gp->destdeg[i] = mo.destdeg[i]; gp->list[i] = mo.list[i]; }
   for (int i = 0; i < 63; i++) gp->fcnt[i] = mo.fcnt[i];
+  for (int i = 0; i < 63; i++) gp->anch[i] = mo.anch[i];
+  gp->nsets = mo.anchorsets;
+  gp->exact = job.exact_placements;
   // placement steps: anchor sets from the last to the first; within a set the
   // regions containing it in increasing bitmap order, the all-anchor region last
   int ns = 0;

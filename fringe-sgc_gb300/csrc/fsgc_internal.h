@@ -89,6 +89,7 @@ struct CountJob {
   int core_type;      // out
   u64 host_value;     // used when the result needs no device work (n, m/2, T)
   bool host_only;
+  int exact_placements;  // general core: exact placement sum instead of the reference's
 };
 
 // Launchers over caller-provided device memory (used by noalloc.cu).

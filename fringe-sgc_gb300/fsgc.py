@@ -100,6 +100,7 @@ def lib():
             "fsgc_ctx_timer_stop": (I, [P, C.POINTER(C.c_double)]),
             "fsgc_ctx_flush_l2": (I, [P, C.c_size_t]),
             "fsgc_ctx_synchronize": (I, [P]),
+            "fsgc_ctx_set_exact_placements": (I, [P, I]),
             "fsgc_count_wedge_noalloc": (I, [I, I64, P, P, C.POINTER(MatchingOrder), P, C.POINTER(Result),
                                              C.c_char_p, I]),
             "fsgc_nck_host": (C.c_ulonglong, [I, I]),
@@ -272,6 +273,9 @@ class Context:
 
     def flush_l2(self, nbytes=0):
         _check(lib().fsgc_ctx_flush_l2(self.ptr, nbytes), "flush_l2", self.ptr)
+
+    def set_exact_placements(self, on):
+        _check(lib().fsgc_ctx_set_exact_placements(self.ptr, 1 if on else 0), "set_exact_placements", self.ptr)
 
     def synchronize(self):
         _check(lib().fsgc_ctx_synchronize(self.ptr), "synchronize", self.ptr)

@@ -128,6 +128,11 @@ int fsgc_ctx_timer_start(fsgc_ctx* ctx);
 int fsgc_ctx_timer_stop(fsgc_ctx* ctx, double* ms);
 int fsgc_ctx_flush_l2(fsgc_ctx* ctx, size_t bytes);
 int fsgc_ctx_synchronize(fsgc_ctx* ctx);
+/* General cores (4-6 core vertices): 0 (default) sums fringe placements the
+ * way the reference's functionX does (src/fringeCount.cu:408-486), which for
+ * anchor sets with two or more fringes can differ from the exact number of
+ * placements; 1 sums the exact number.  Other core types are unaffected. */
+int fsgc_ctx_set_exact_placements(fsgc_ctx* ctx, int on);
 
 /* ---- resident graphs (CSR upload + loader: src/fringeCount.cu:2286-2297) ---- */
 

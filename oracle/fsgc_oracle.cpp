@@ -544,6 +544,62 @@ static u64 place(GenCtx& c, int asi, int idx, int remaining) {
   return s;
 }
 
+// functionX with the reference's own control flow (src/fringeCount.cu:408-486):
+// a flat depth-first walk that saves (a, prod, region, venn[region], fr[set])
+// per level and, when it backs up, restores only the level it returns to.  A
+// region changed by the step it abandons keeps that change, so later
+// alternatives can see a reduced region size; for anchor sets with two or
+// more fringes this gives different sums than placement() above (the exact
+// count), and this is what the reference computes.
+static u64 place_reference(GenCtx& c, int* fr) {
+  const MO& mo = *c.mo;
+  const int top = c.anchors, non = c.nonanchors;
+  static thread_local int savea[665], saveidx[665], savevenn[665];
+  static thread_local u64 saveprod[665];
+  static thread_local int savefr[665];
+  int asi = mo.anchorsets - 1;
+  u64 sum = 0, prod = 1;
+  int level = 0;
+  int anch = mo.anch[asi];
+  int idx = anch;
+  int a = std::min(c.venn[idx], fr[anch]);
+  for (;;) {
+    savea[level] = a; saveprod[level] = prod; saveidx[level] = idx;
+    savevenn[level] = c.venn[idx]; savefr[level] = fr[anch];
+    if (a < 0) {
+      prod = 0;
+    } else if (idx == top) {
+      prod *= nck(c.venn[idx], fr[anch]);
+      c.venn[idx] -= fr[anch];
+      fr[anch] = 0;
+      if (asi == 0) { sum += prod; prod = 0; }
+    } else {
+      prod *= nck(c.venn[idx], a);
+      c.venn[idx] -= a;
+      fr[anch] -= a;
+    }
+    if (prod == 0) {
+      level--;
+      if (level < 0) break;
+      a = savea[level] - 1;
+      prod = saveprod[level];
+      idx = saveidx[level];
+      if (idx == top) { asi++; anch = mo.anch[asi]; }
+      c.venn[idx] = savevenn[level];
+      fr[anch] = savefr[level];
+    } else {
+      level++;
+      if (idx == top) { asi--; anch = mo.anch[asi]; idx = anch; }
+      else idx = (((idx | non) + 1) | anch) & ~non;
+      a = (idx == top) ? 0 : std::min(c.venn[idx], fr[anch]);
+    }
+  }
+  fr[mo.anch[mo.anchorsets - 1]] = savefr[0];
+  return sum;
+}
+
+static int g_exact_placements = 0;  // 1: exact placement sum, 0: the reference's functionX
+
 static u64 gen_dfs(GenCtx& c, int level) {
   // choose stack[level+1]
   const MO& mo = *c.mo;
@@ -567,7 +623,13 @@ static u64 gen_dfs(GenCtx& c, int level) {
     c.stack[level + 1] = x;
     if (level + 1 == c.k - 1) {
       venn_general(c);
-      sum += place_set(c, mo.anchorsets - 1);
+      if (g_exact_placements) {
+        sum += place_set(c, mo.anchorsets - 1);
+      } else {
+        int fr[64] = {0};
+        for (int i = 0; i < mo.anchorsets; i++) fr[mo.anch[i]] = mo.fcnt[i];
+        sum += place_reference(c, fr);
+      }
     } else {
       sum += gen_dfs(c, level + 1);
     }
@@ -680,6 +742,10 @@ int oracle_count(int n, const long long* idx, const int* adj, const unsigned cha
   out[3] = (u64)ct;
   return 0;
 }
+
+// General-core placement sums: 0 (default) follows the reference's functionX
+// exactly, 1 computes the exact number of fringe placements.
+void oracle_set_exact_placements(int on) { g_exact_placements = on ? 1 : 0; }
 
 // Per-call building blocks exposed for unit tests.
 unsigned long long oracle_nck(int n, int k) { return nck(n, k); }

@@ -32,6 +32,8 @@ def lib():
         L.oracle_count.restype = C.c_int
         L.oracle_count.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int,
                                    C.POINTER(C.c_ulonglong)]
+        L.oracle_set_exact_placements.restype = None
+        L.oracle_set_exact_placements.argtypes = [C.c_int]
         L.oracle_nck.restype = C.c_ulonglong
         L.oracle_nck.argtypes = [C.c_int, C.c_int]
         L.oracle_fc3.restype = C.c_ulonglong
@@ -45,8 +47,11 @@ def lib():
     return _lib
 
 
-def count(nindex, nlist, mo_bytes, stride=1, phase=0, threads=0):
-    """Reference-semantics count: dict(count, raw, aut, core)."""
+def count(nindex, nlist, mo_bytes, stride=1, phase=0, threads=0, exact_placements=False):
+    """Reference-semantics count: dict(count, raw, aut, core).  With
+    exact_placements the general core sums the exact number of fringe
+    placements instead of following the reference's functionX."""
+    lib().oracle_set_exact_placements(1 if exact_placements else 0)
     idx = np.ascontiguousarray(nindex, dtype=np.int64)
     adj = np.ascontiguousarray(nlist, dtype=np.int32)
     if len(adj) == 0:
@@ -54,6 +59,7 @@ def count(nindex, nlist, mo_bytes, stride=1, phase=0, threads=0):
     out = (C.c_ulonglong * 4)()
     st = lib().oracle_count(len(idx) - 1, idx.ctypes.data, adj.ctypes.data, bytes(mo_bytes), stride, phase,
                             threads, out)
+    lib().oracle_set_exact_placements(0)
     if st != 0:
         raise RuntimeError(f"oracle_count failed ({st})")
     return {"count": out[0], "raw": out[1], "aut": out[2], "core": out[3]}

@@ -104,6 +104,37 @@ def test_wrapping_patterns_on_hub(ctx, hub_id):
         ctx.release(gid)
 
 
+def test_exact_placement_mode(ctx):
+    """With exact placements, general-core counts equal the oracle's exact mode
+    (and so the brute-force count on small graphs)."""
+    g = graph("er300")
+    gid = ctx.upload(g)
+    ctx.set_exact_placements(True)
+    try:
+        for name, mo in mos():
+            if mo.nodes < 4:
+                continue
+            r = ctx.count(gid, mo)
+            o = oracle.count(g.nindex, g.nlist, mo.to_bytes(), exact_placements=True)
+            assert (r.count, r.raw_total, r.automorphisms) == (o["count"], o["raw"], o["aut"]), name
+    finally:
+        ctx.set_exact_placements(False)
+        ctx.release(gid)
+    small = fsgc.gen_er(14, 40, 9)
+    gid = ctx.upload(small)
+    ctx.set_exact_placements(True)
+    try:
+        for name, (n, e) in {**WORKLOAD, **EXTRA}.items():
+            if n > 8:
+                continue
+            mo = fsgc.preprocess(n, e)
+            b, _ = oracle.bruteforce(small.nindex, small.nlist, n, e)
+            assert ctx.count(gid, mo).count == b, name
+    finally:
+        ctx.set_exact_placements(False)
+        ctx.release(gid)
+
+
 def test_batch_equals_single_counts(ctx):
     g = graph("rmat10")
     g2 = graph("er300")
