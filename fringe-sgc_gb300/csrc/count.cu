@@ -463,27 +463,37 @@ struct WedgeParams {
 // BIG (hub endpoints): 32-bit counters, cursors in a per-block global array.
 constexpr int kWDvMax = 2048;
 constexpr int kWThreads = 1024;
-constexpr int kWBuf = 96;  // per-warp pair buffer (flushed 32 at a time)
+constexpr int kWGran = 32768;  // ids between the chunk boundaries in the boundary table
 
 template <bool BIG>
 struct WedgeCfg {
-  static constexpr int CH = BIG ? 32768 : 65536;          // ids per chunk
-  static constexpr int WORDS = BIG ? CH : CH / 2;         // counter words
+  static constexpr int CH = BIG ? 32768 : 65536;   // ids per chunk (multiple of kWGran)
+  static constexpr int WORDS = BIG ? CH : CH / 2;  // counter words
+  static constexpr int TW = WORDS / 32;            // touched-bitmap words (= kWThreads)
 };
+static_assert(WedgeCfg<false>::TW == kWThreads && WedgeCfg<true>::TW == kWThreads, "one bitmap word per thread");
 
 template <bool BIG>
 struct WedgeSmem {
   unsigned cnt[WedgeCfg<BIG>::WORDS];
-  unsigned touched[WedgeCfg<BIG>::WORDS / 32];  // counter words that became non-zero
+  unsigned touched[WedgeCfg<BIG>::TW];  // counter words that became non-zero
+  int tpre[WedgeCfg<BIG>::TW + 1];      // prefix of touched popcounts
   unsigned adjbits[WedgeCfg<BIG>::CH / 32];
   long long cur[BIG ? 1 : kWDvMax];
   long long lim[BIG ? 1 : kWDvMax];
   int pre[BIG ? 1 : kWDvMax + 1];
-  int buf_o[32][kWBuf];
-  unsigned buf_c[32][kWBuf];
   int warp_tmp[33];
   int v;
   int lo;
+};
+
+// Per high-degree vertex u: offsets in N(u) of the first neighbour >= k *
+// kWGran, for every k.  A chunk that ends on such a boundary finds the end of
+// u's segment with one load instead of a search.
+struct ChunkTable {
+  const int* id;   // n entries: row of u, or -1
+  const int* pos;  // rows of K offsets
+  int K;
 };
 
 // first index i in [from, to) with a[i] >= x, searching outward from `from`
@@ -540,24 +550,32 @@ __device__ void block_scan_inplace(int* x, int n, WedgeSmem<BIG>& S) {
 }
 
 template <bool BIG>
+__device__ __forceinline__ void eval_pair(const GView& g, const WedgeParams& p, WedgeSmem<BIG>& S, int lo, int o,
+                                          unsigned C, int dw, int dv, int thres, u64& acc) {
+  if (dw >= thres) {
+    const bool vw = (S.adjbits[o >> 5] >> (o & 31)) & 1u;
+    acc += (u64)C * wedge_formula(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1);
+  }
+}
+
+template <bool BIG>
 __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, WedgeParams p, int* __restrict__ queue,
                                                                    long long* __restrict__ gcur, int* __restrict__ gpre,
-                                                                   long long gstride, u64* __restrict__ slot) {
+                                                                   long long gstride, ChunkTable tab,
+                                                                   u64* __restrict__ slot) {
   constexpr int CH = WedgeCfg<BIG>::CH;
   constexpr int WORDS = WedgeCfg<BIG>::WORDS;
+  constexpr int TW = WedgeCfg<BIG>::TW;
   extern __shared__ unsigned char s_raw[];
   WedgeSmem<BIG>& S = *reinterpret_cast<WedgeSmem<BIG>*>(s_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-  const unsigned lt = (1u << lane) - 1u;
   long long* cur = BIG ? gcur + (size_t)blockIdx.x * 2 * gstride : S.cur;
   long long* lim = BIG ? cur + gstride : S.lim;
   int* pre = BIG ? gpre + (size_t)blockIdx.x * (gstride + 1) : S.pre;
   for (int i = tid; i < WORDS; i += blockDim.x) S.cnt[i] = 0;
-  for (int i = tid; i < WORDS / 32; i += blockDim.x) S.touched[i] = 0;
+  for (int i = tid; i < TW; i += blockDim.x) S.touched[i] = 0;
   for (int i = tid; i < CH / 32; i += blockDim.x) S.adjbits[i] = 0;
   u64 acc = 0;
-  int* bo = S.buf_o[warp];
-  unsigned* bc = S.buf_c[warp];
   for (;;) {
     if (tid == 0) {
       S.v = atomicAdd(queue, 1);
@@ -582,11 +600,21 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
     int cv = 0;  // cursor into N(v) for the adjacency marks
     __syncthreads();
     while (S.lo < v) {
-      const int lo = S.lo;
+      const int lo = S.lo;  // a multiple of CH
       const int hi = min(lo + CH, v);
+      const bool aligned = (hi % kWGran) == 0;
+      // segment of each centre's list inside [lo, hi): table lookup for
+      // high-degree centres at aligned chunk ends, a gallop from the cursor otherwise
       for (int t = tid; t < dv; t += blockDim.x) {
         const long long c = cur[t];
-        pre[t] = (int)(gallop_lb(g.adj, c, lim[t], hi) - c);
+        long long e = -1;
+        if (aligned && tab.id) {
+          const int u = __ldg(Nv + t);
+          const int row = __ldg(tab.id + u);
+          if (row >= 0) e = g.off[u] + __ldg(tab.pos + (size_t)row * tab.K + hi / kWGran);
+        }
+        if (e < 0) e = gallop_lb(g.adj, c, lim[t], hi);
+        pre[t] = (int)(e - c);
       }
       const int cs = cv + lower_bound_dev(Nv + cv, dv - cv, lo);
       const int cend = cs + lower_bound_dev(Nv + cs, dv - cs, hi);
@@ -623,74 +651,62 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
         }
       }
       __syncthreads();
-      // evaluate: warps take ranges of the touched-word bitmap; each lane walks
-      // the set bits of one bitmap word; non-zero counters are compacted so
-      // that every lane evaluates one pair per flush
+      // evaluate: prefix-sum the touched-word popcounts (one bitmap word per
+      // thread) and give every thread an equal share of the touched words
       {
         const int nw = BIG ? (hi - lo) : ((hi - lo + 1) >> 1);
-        const int nt = (nw + 31) >> 5;
-        const int ws = (int)(((long long)nt * warp) / nwarp), we = (int)(((long long)nt * (warp + 1)) / nwarp);
-        int nb = 0;
-        auto flush = [&](int count) {
-          if (lane < count) {
-            const int o = bo[lane];
-            const unsigned C = bc[lane];
-            const int w = lo + o;
-            const int dw = g.deg[w];
-            if (dw >= thres) {
-              const bool vw = (S.adjbits[o >> 5] >> (o & 31)) & 1u;
-              acc += (u64)C * wedge_formula(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1);
-            }
+        const int ntw = (nw + 31) >> 5;
+        const int c0 = (tid < ntw) ? __popc(S.touched[tid]) : 0;
+        int inc = c0;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, inc, o);
+          if (lane >= o) inc += y;
+        }
+        if (lane == 31) S.warp_tmp[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+          const int wv = (lane < nwarp) ? S.warp_tmp[lane] : 0;
+          int wi = wv;
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
           }
-        };
-        for (int t0 = ws; t0 < we; t0 += 32) {
-          const int t = t0 + lane;
-          unsigned mask = 0;
-          if (t < we) {
-            mask = S.touched[t];
-            if (mask) S.touched[t] = 0;
+          if (lane < nwarp) S.warp_tmp[lane] = wi - wv;
+          if (lane == 31) S.warp_tmp[32] = wi;
+        }
+        __syncthreads();
+        S.tpre[tid] = S.warp_tmp[warp] + inc - c0;
+        const int T = S.warp_tmp[32];
+        __syncthreads();
+        const int r0 = (int)(((long long)T * tid) / blockDim.x), r1 = (int)(((long long)T * (tid + 1)) / blockDim.x);
+        if (r0 < r1) {
+          int a = 0, b = ntw;  // bitmap word holding rank r0: last with tpre <= r0
+          while (b - a > 1) {
+            const int mid = (a + b) >> 1;
+            if (S.tpre[mid] <= r0) a = mid;
+            else b = mid;
           }
-          while (__any_sync(0xffffffffu, mask != 0)) {
-            unsigned word = 0;
-            int wd = 0;
-            if (mask) {
-              const int b = __ffs(mask) - 1;
-              mask &= mask - 1;
-              wd = (t << 5) + b;
-              word = S.cnt[wd];
-              S.cnt[wd] = 0;
-            }
-            constexpr int PER = BIG ? 1 : 2;
-#pragma unroll
-            for (int h = 0; h < PER; h++) {
-              const unsigned C = BIG ? word : ((word >> (16 * h)) & 0xffffu);
-              const bool has = C != 0;
-              const unsigned bal = __ballot_sync(0xffffffffu, has);
-              if (has) {
-                const int q = nb + __popc(bal & lt);
-                bo[q] = BIG ? wd : 2 * wd + h;
-                bc[q] = C;
-              }
-              nb += __popc(bal);
-            }
-            __syncwarp();
-            while (nb >= 32) {
-              flush(32);
-              __syncwarp();
-              const int rest = nb - 32;
-              for (int q = lane; q < rest; q += 32) {
-                const int oo = bo[32 + q];  // 32 + q > q: no lane reads what another writes
-                const unsigned cc = bc[32 + q];
-                bo[q] = oo;
-                bc[q] = cc;
-              }
-              __syncwarp();
-              nb = rest;
+          unsigned mask = S.touched[a];
+          for (int k = r0 - S.tpre[a]; k > 0; k--) mask &= mask - 1;
+          for (int r = r0; r < r1; r++) {
+            while (mask == 0) mask = S.touched[++a];
+            const int wd = (a << 5) + (__ffs(mask) - 1);
+            mask &= mask - 1;
+            const unsigned word = S.cnt[wd];
+            S.cnt[wd] = 0;
+            if (BIG) {
+              const int w = lo + wd;
+              eval_pair<BIG>(g, p, S, lo, wd, word, g.deg[w], dv, thres, acc);
+            } else {
+              const int o0 = 2 * wd;
+              const unsigned C0 = word & 0xffffu, C1 = word >> 16;
+              const int d0 = C0 ? g.deg[lo + o0] : 0;
+              const int d1 = C1 ? g.deg[lo + o0 + 1] : 0;
+              if (C0) eval_pair<BIG>(g, p, S, lo, o0, C0, d0, dv, thres, acc);
+              if (C1) eval_pair<BIG>(g, p, S, lo, o0 + 1, C1, d1, dv, thres, acc);
             }
           }
         }
-        flush(nb);
-        __syncwarp();
       }
       // advance the cursors and find the next id any centre still reaches
       int nxt = 0x7fffffff;
@@ -702,13 +718,39 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
       nxt = __reduce_min_sync(0xffffffffu, nxt);
       cv = cend;
       if (tid == 0) S.lo = v;
-      __syncthreads();  // adjbits, pre and S.lo are free again
+      __syncthreads();  // touched, adjbits, pre and S.lo are free again
+      for (int i = tid; i < TW; i += blockDim.x) S.touched[i] = 0;
       for (int i = tid; i < (CH >> 5); i += blockDim.x) S.adjbits[i] = 0;
-      if (lane == 0) atomicMin(&S.lo, max(hi, nxt));
+      if (lane == 0 && nxt < v) atomicMin(&S.lo, max(hi, (nxt / CH) * CH));
       __syncthreads();
     }
   }
   block_sum_to(acc, slot);
+}
+
+// boundary table: pass 1 gives each vertex of degree >= min_deg a row
+__global__ void chunk_table_rows_kernel(GView g, int min_deg, int* __restrict__ id, int* __restrict__ rows,
+                                        int* __restrict__ nrows) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < g.n; u += gridDim.x * blockDim.x) {
+    int r = -1;
+    if (g.deg[u] >= min_deg) {
+      r = atomicAdd(nrows, 1);
+      rows[r] = u;
+    }
+    id[u] = r;
+  }
+}
+
+// pass 2: row r, column k = first position in N(rows[r]) with neighbour >= k * kWGran
+__global__ void chunk_table_fill_kernel(GView g, const int* __restrict__ rows, int nrows, int K, int* __restrict__ pos) {
+  const long long total = (long long)nrows * K;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / K), k = (int)(i % K);
+    const int u = rows[r];
+    const long long b = g.off[u];
+    const long long x = (long long)k * kWGran;
+    pos[i] = (x > 0x7fffffffLL) ? (int)(g.off[u + 1] - b) : lower_bound_dev(g.adj + b, (int)(g.off[u + 1] - b), (int)x);
+  }
 }
 
 struct GWedgeParams {
@@ -1095,6 +1137,43 @@ int grid_for(long long work, int tpb, int per_sm) {
   return (int)std::max(1LL, std::min(want, cap));
 }
 
+// Builds the wedge core's chunk-boundary table once per graph (vertices of
+// degree >= 512, fewer when the table would pass 512 MiB).
+int ensure_chunk_table(DevGraph& G, cudaStream_t s, uint64_t* launches, u64* d_small) {
+  if (G.ctab_K > 0) return FSGC_OK;
+  const int K = (int)(((long long)G.n + kWGran - 1) / kWGran) + 1;
+  int min_deg = 512;
+  GView gv = G.view();
+  int* nrows_d = reinterpret_cast<int*>(d_small);
+  if (cudaMalloc((void**)&G.ctab_id, sizeof(int) * (size_t)std::max(1, G.n)) != cudaSuccess ||
+      cudaMalloc((void**)&G.ctab_rows, sizeof(int) * (size_t)std::max(1, G.n)) != cudaSuccess) {
+    cudaGetLastError();
+    return FSGC_ENOMEM;
+  }
+  int nrows = 0;
+  for (;;) {
+    cudaMemsetAsync(nrows_d, 0, sizeof(int), s);
+    chunk_table_rows_kernel<<<grid_for(G.n, 256, 8), 256, 0, s>>>(gv, min_deg, G.ctab_id, G.ctab_rows, nrows_d);
+    *launches += 1;
+    if (cudaMemcpyAsync(&nrows, nrows_d, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return FSGC_ECUDA;
+    if ((size_t)nrows * K * sizeof(int) <= ((size_t)512 << 20)) break;
+    min_deg *= 2;
+  }
+  if (cudaMalloc((void**)&G.ctab_pos, sizeof(int) * std::max<size_t>(1, (size_t)nrows * K)) != cudaSuccess) {
+    cudaGetLastError();
+    return FSGC_ENOMEM;
+  }
+  if (nrows > 0) {
+    chunk_table_fill_kernel<<<grid_for((long long)nrows * K, 256, 8), 256, 0, s>>>(gv, G.ctab_rows, nrows, K, G.ctab_pos);
+    *launches += 1;
+  }
+  G.ctab_K = K;
+  G.bytes += sizeof(int) * ((size_t)2 * G.n + (size_t)nrows * K);
+  return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+
 int ensure_plain_scratch(Scratch& sc, size_t need, cudaStream_t s) {
   if (sc.bytes >= need) return FSGC_OK;
   if (sc.ptr) {
@@ -1184,12 +1263,15 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
       WedgeParams wp{f[IV], f[IVW], f[IW], lim, min_v + min_w};
       int* q1 = reinterpret_cast<int*>(work.small + 7);
       int* q2 = reinterpret_cast<int*>(work.small + 8);
+      st = ensure_chunk_table(G, s, launches, work.small + 9);
+      if (st != FSGC_OK) return st;
+      const ChunkTable tab{G.ctab_id, G.ctab_pos, G.ctab_K};
       cudaMemsetAsync(q1, 0, 2 * sizeof(u64), s);
       const int blocks = sm_count();
       {
         const size_t smem = sizeof(WedgeSmem<false>);
         cudaFuncSetAttribute(wedge_chunk_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        wedge_chunk_kernel<false><<<blocks, kWThreads, smem, s>>>(gv, wp, q1, nullptr, nullptr, 0, job.d_slot);
+        wedge_chunk_kernel<false><<<blocks, kWThreads, smem, s>>>(gv, wp, q1, nullptr, nullptr, 0, tab, job.d_slot);
         *launches += 1;
       }
       if (G.maxdeg > kWDvMax) {
@@ -1202,7 +1284,7 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
         int* gpre = reinterpret_cast<int*>(gcur + (size_t)blocks * 2 * gs);
         const size_t smem = sizeof(WedgeSmem<true>);
         cudaFuncSetAttribute(wedge_chunk_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        wedge_chunk_kernel<true><<<blocks, kWThreads, smem, s>>>(gv, wp, q2, gcur, gpre, gs, job.d_slot);
+        wedge_chunk_kernel<true><<<blocks, kWThreads, smem, s>>>(gv, wp, q2, gcur, gpre, gs, tab, job.d_slot);
         *launches += 1;
       }
       return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
@@ -1303,7 +1385,8 @@ int launch_wedge_small(const GView& gv, int f_v, int f_vw, int f_w, int lim, int
   WedgeParams wp{f_v, f_vw, f_w, lim, minsum};
   const size_t smem = sizeof(WedgeSmem<false>);
   cudaFuncSetAttribute(wedge_chunk_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  wedge_chunk_kernel<false><<<sm_count(), kWThreads, smem, s>>>(gv, wp, queue, nullptr, nullptr, 0, slot);
+  wedge_chunk_kernel<false><<<sm_count(), kWThreads, smem, s>>>(gv, wp, queue, nullptr, nullptr, 0,
+                                                                ChunkTable{nullptr, nullptr, 0}, slot);
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }
 
@@ -1312,7 +1395,8 @@ int launch_wedge_big(const GView& gv, int f_v, int f_vw, int f_w, int lim, int m
   WedgeParams wp{f_v, f_vw, f_w, lim, minsum};
   const size_t smem = sizeof(WedgeSmem<true>);
   cudaFuncSetAttribute(wedge_chunk_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  wedge_chunk_kernel<true><<<blocks, kWThreads, smem, s>>>(gv, wp, queue, gcur, gpre, gstride, slot);
+  wedge_chunk_kernel<true><<<blocks, kWThreads, smem, s>>>(gv, wp, queue, gcur, gpre, gstride,
+                                                           ChunkTable{nullptr, nullptr, 0}, slot);
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }
 

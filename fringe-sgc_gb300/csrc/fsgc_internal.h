@@ -44,6 +44,11 @@ struct DevGraph {
   long long max_outdeg = 0;        // largest oriented out-degree
   long long max_bitmap_words = 0;  // max over v of outdeg(v) * ceil(deg(v) / 32)
   u64* vtri2 = nullptr;  // lazily
+  // wedge core: offsets of chunk boundaries in the lists of high-degree vertices (lazily)
+  int* ctab_id = nullptr;
+  int* ctab_rows = nullptr;
+  int* ctab_pos = nullptr;
+  int ctab_K = 0;
   // the reference's degree-relabel gate for the triangle core
   // (src/fringeCount.cu:1237, 1342-1344): vertex roles follow (deg, id) order
   // when it fires, vertex ids otherwise

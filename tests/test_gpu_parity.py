@@ -135,6 +135,30 @@ def test_exact_placement_mode(ctx):
         ctx.release(gid)
 
 
+def test_wedge_chunks_over_large_id_ranges(ctx):
+    """Vertex ids beyond 64K and hubs above degree 512/2048: the wedge kernels
+    sweep several id chunks per endpoint and read the chunk-boundary table."""
+    rng = np.random.default_rng(11)
+    n = 100000
+    hubs = {99999: 2100, 50000: 1500, 70001: 900}
+    pairs = []
+    for h, k in hubs.items():
+        leaves = rng.choice(n, size=k, replace=False)
+        pairs += [(h, int(x)) for x in leaves if x != h]
+    pairs += list(zip(rng.integers(0, n, 60000).tolist(), rng.integers(0, n, 60000).tolist()))
+    g = fsgc.csr_from_edges(n, pairs)
+    gid = ctx.upload(g)
+    try:
+        for name in ("wedge_1_on_each_end", "4cycle_opposite"):
+            check(ctx, g, gid, name, fsgc.preprocess(*WORKLOAD[name]))
+        for name in ("edge_8_3", "star_12"):
+            check(ctx, g, gid, name, fsgc.preprocess(*EXTRA[name]))
+        wedge_ends = fsgc.preprocess(11, [(0, 1), (0, 2)] + [(1, i) for i in range(3, 10)] + [(2, 10)])
+        check(ctx, g, gid, "wedge_ends_7_1", wedge_ends)
+    finally:
+        ctx.release(gid)
+
+
 def test_batch_equals_single_counts(ctx):
     g = graph("rmat10")
     g2 = graph("er300")

@@ -96,3 +96,29 @@ def test_counts_match_reference_kernels(ctx, gname, tmp_path):
                    (r["count"], r["raw"], r["aut"], want_core), (gname, name, r)
     finally:
         ctx.release(gid)
+
+
+def test_bench_patterns_rmat16_match_reference_kernels(ctx, tmp_path):
+    """The eight RMAT workload patterns at scale 16 (n = 65,536, hubs of degree
+    up to ~9,700): fsgc and the reference's kernels agree bit for bit."""
+    g = fsgc.gen_rmat(16, 16, 0.57, 0.19, 0.19, 20251203)
+    egr = str(tmp_path / "g.egr")
+    fsgc.egr_write(egr, g)
+    names = ["wedge_1_on_centre", "wedge_2_on_centre", "wedge_4_on_centre", "wedge_1_on_each_end",
+             "triangle_3_on_one", "4cycle_opposite", "4clique_3_distinct", "edge_5_5"]
+    mos = [fsgc.preprocess(*WORKLOAD[n]) for n in names]
+    paths = []
+    for i, mo in enumerate(mos):
+        p = str(tmp_path / f"b{i}.mo")
+        with open(p, "wb") as f:
+            f.write(mo.to_bytes())
+        paths.append(p)
+    ref = run_reference(egr, paths)
+    gid = ctx.upload(g)
+    try:
+        for name, mo, r in zip(names, mos, ref):
+            got = ctx.count(gid, mo)
+            assert (got.count, got.raw_total, got.automorphisms, got.core_type) == \
+                   (r["count"], r["raw"], r["aut"], r["core"]), name
+    finally:
+        ctx.release(gid)
