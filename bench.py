@@ -147,6 +147,22 @@ def kernel_bytes(name, core, g):
     return None
 
 
+def max_over_ranks(values, world):
+    """Replicas: the job's time is the slowest rank's (element-wise max over ranks)."""
+    if world <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def job_value(patterns_per_rank, steps, world, seconds):
+    """Whole-job throughput: every rank counts the whole workload (replicas)."""
+    return patterns_per_rank * world * steps / seconds
+
+
 def run_gpu(args, rank, world):
     import fsgc
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -221,12 +237,7 @@ def run_gpu(args, rank, world):
     barrier()
     for a, b in zip(res_h, ref_res):
         assert a.count == b.count
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev, t_e2e = float(tt[0]), float(tt[1])
+    t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], world)
     out = {
         "per_task_ms": {name: per_task[i] / args.steps for i, (name, _) in enumerate(mos)},
         "prep_ms": statistics.mean(prep_ms),
@@ -317,9 +328,8 @@ def main():
         if world > 1:
             __import__("torch").distributed.destroy_process_group()
         return
-    n_pat = len(mos) * world
-    value = n_pat * args.steps / out["t_dev"]
-    e2e = n_pat * args.steps / out["t_e2e"]
+    value = job_value(len(mos), args.steps, world, out["t_dev"])
+    e2e = job_value(len(mos), args.steps, world, out["t_e2e"])
     peak, peak_kind = load_peaks()
     # dominant kernel: the task with the largest device time
     dom = max(out["per_task_ms"], key=out["per_task_ms"].get)

@@ -36,6 +36,9 @@ struct fsgc_ctx {
   std::map<std::string, u64> aut_cache;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   int exact_placements = 0;
+  u64* d_member = nullptr;  // per-member result slots of packed counts
+  u64* h_member = nullptr;
+  int member_cap = 0;
   void* flush_buf = nullptr;
   size_t flush_bytes = 0;
 };
@@ -78,6 +81,8 @@ void free_graph(DevGraph* g) {
   cudaFree(g->ctab_id);
   cudaFree(g->ctab_rows);
   cudaFree(g->ctab_pos);
+  cudaFree(g->comp);
+  cudaFree(g->comp_relabel);
   delete g;
 }
 
@@ -87,6 +92,8 @@ int ensure_slots(fsgc_ctx* c, int n) {
   cudaStreamSynchronize(c->stream);
   cudaFree(c->d_slots);
   cudaFreeHost(c->h_slots);
+  cudaFree(c->d_member);
+  cudaFreeHost(c->h_member);
   c->d_slots = nullptr;
   c->h_slots = nullptr;
   CK(cudaMalloc((void**)&c->d_slots, sizeof(u64) * (size_t)cap), "slot allocation");
@@ -190,7 +197,7 @@ int automorphisms(fsgc_ctx* c, const fsgc_matching_order& mo, u64* out) {
   st = ensure_slots(c, 1);
   if (st != FSGC_OK) { free_graph(pg); return st; }
   cudaMemsetAsync(c->d_slots, 0, sizeof(u64), c->stream);
-  fsgc::CountJob job{&mo, pg, c->d_slots, 0, 0, false, c->exact_placements};
+  fsgc::CountJob job{&mo, pg, c->d_slots, 0, 0, false, c->exact_placements, nullptr, 1};
   st = fsgc::enqueue_count(job, c->stream, &c->launches, c->work);
   u64 raw = 0;
   if (st == FSGC_OK) {
@@ -245,6 +252,7 @@ int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
     if (!mo_valid(mo)) return fail(c, FSGC_EINVAL, "task %d: malformed matching order", t);
     DevGraph* g = find_graph(c, tasks[t].gid);
     if (!g) return fail(c, FSGC_ENOTFOUND, "task %d: unknown graph %d", t, tasks[t].gid);
+    if (g->ngraphs > 0) return fail(c, FSGC_EINVAL, "task %d: graph %d is packed; use fsgc_count_packed", t, tasks[t].gid);
     if (mo.nodes >= 3 && !pattern_too_large(mo, *g)) {
       st = automorphisms(c, mo, &aut[t]);
       if (st != FSGC_OK) return st;
@@ -255,7 +263,7 @@ int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
   for (int t = 0; t < nt; t++) {
     const fsgc_matching_order& mo = tasks[t].mo;
     DevGraph* g = find_graph(c, tasks[t].gid);
-    jobs[t] = fsgc::CountJob{&tasks[t].mo, g, c->d_slots + t, 0, 0, false, c->exact_placements};
+    jobs[t] = fsgc::CountJob{&tasks[t].mo, g, c->d_slots + t, 0, 0, false, c->exact_placements, nullptr, 1};
     if (pattern_too_large(mo, *g)) {
       jobs[t].host_only = true;
       jobs[t].host_value = 0;
@@ -341,6 +349,8 @@ void fsgc_ctx_destroy(fsgc_ctx* c) {
   cudaFree(c->work.tri.ptr);
   cudaFree(c->d_slots);
   cudaFreeHost(c->h_slots);
+  cudaFree(c->d_member);
+  cudaFreeHost(c->h_member);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -461,6 +471,131 @@ int fsgc_graph_release(fsgc_ctx* c, int gid) {
   cudaStreamSynchronize(c->stream);
   free_graph(it->second);
   c->graphs.erase(it);
+  return FSGC_OK;
+}
+
+int fsgc_graph_from_packed_csr(fsgc_ctx* c, int n, int64_t m, const int64_t* nindex, const int32_t* nlist,
+                               int ngraphs, const int32_t* vstart, int* gid) {
+  if (!c || !gid || n < 1 || m < 0 || !nindex || (m > 0 && !nlist) || ngraphs < 1 || !vstart)
+    return fail(c, FSGC_EINVAL, "bad packed graph arguments");
+  if (vstart[0] != 0 || vstart[ngraphs] != n) return fail(c, FSGC_EINVAL, "member ranges must cover [0, n)");
+  if (nindex[0] != 0 || nindex[n] != m) return fail(c, FSGC_EINVAL, "offsets must start at 0 and end at m");
+  std::vector<int> comp((size_t)n);
+  std::vector<unsigned char> relabel((size_t)ngraphs);
+  std::vector<int> mn((size_t)ngraphs);
+  std::vector<long long> mm((size_t)ngraphs);
+  for (int gi = 0; gi < ngraphs; gi++) {
+    const int a = vstart[gi], b = vstart[gi + 1];
+    if (b <= a) return fail(c, FSGC_EINVAL, "member graph %d is empty", gi);
+    int maxd = 0;
+    for (int v = a; v < b; v++) {
+      comp[v] = gi;
+      if (nindex[v + 1] < nindex[v]) return fail(c, FSGC_EINVAL, "offsets decrease at vertex %d", v);
+      maxd = std::max(maxd, (int)(nindex[v + 1] - nindex[v]));
+      for (int64_t j = nindex[v]; j < nindex[v + 1]; j++)
+        if (nlist[j] < a || nlist[j] >= b) return fail(c, FSGC_EINVAL, "edge %d-%d crosses member graphs", v, nlist[j]);
+    }
+    mn[gi] = b - a;
+    mm[gi] = nindex[b] - nindex[a];
+    // the triangle core's relabel gate, per member (src/fringeCount.cu:1237, 1342-1344)
+    relabel[gi] = (mn[gi] > 10000) && !((long long)mn[gi] > mm[gi] / 10) && (maxd > 16);
+  }
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DevGraph* g = nullptr;
+  int st = upload_graph(c, n, m, (const long long*)nindex, nlist, false, &g);
+  if (st != FSGC_OK) return st;
+  cudaError_t e = cudaMalloc((void**)&g->comp, sizeof(int) * (size_t)n);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&g->comp_relabel, (size_t)ngraphs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g->comp, comp.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g->comp_relabel, relabel.data(), (size_t)ngraphs, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    free_graph(g);
+    return cuda_fail(c, e, "packed graph upload");
+  }
+  g->ngraphs = ngraphs;
+  g->member_n = mn;
+  g->member_m = mm;
+  g->bytes += sizeof(int) * (size_t)n + (size_t)ngraphs;
+  *gid = c->next_gid++;
+  c->graphs[*gid] = g;
+  return FSGC_OK;
+}
+
+int fsgc_count_packed(fsgc_ctx* c, int gid, const fsgc_matching_order* mo, fsgc_result* results) {
+  if (!c || !mo || !results) return fail(c, FSGC_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DevGraph* g = find_graph(c, gid);
+  if (!g) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", gid);
+  if (g->ngraphs == 0) return fail(c, FSGC_EINVAL, "graph %d is not packed", gid);
+  if (!mo_valid(*mo)) return fail(c, FSGC_EINVAL, "malformed matching order");
+  const int ng = g->ngraphs;
+  // pattern size (vertices, directed entries) for the per-member early return
+  long long pn = mo->nodes, pm = 0;
+  for (int i = 0; i + 1 < mo->nodes; i++) pm += 2 * __builtin_popcount(mo->list[i]);
+  for (int i = 0; i < mo->anchorsets; i++) {
+    pn += mo->fcnt[i];
+    pm += 2LL * mo->fcnt[i] * __builtin_popcount(mo->anch[i]);
+  }
+  bool any_fits = false;
+  for (int i = 0; i < ng; i++) any_fits = any_fits || !(pn > g->member_n[i] || pm > g->member_m[i]);
+  u64 aut = 1;
+  if (mo->nodes >= 3 && any_fits) {
+    const int st = automorphisms(c, *mo, &aut);
+    if (st != FSGC_OK) return st;
+  }
+  if (ng > c->member_cap) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_member);
+    cudaFreeHost(c->h_member);
+    c->d_member = nullptr;
+    c->h_member = nullptr;
+    c->member_cap = 0;
+    CK(cudaMalloc((void**)&c->d_member, sizeof(u64) * (size_t)ng), "member slots");
+    CK(cudaMallocHost((void**)&c->h_member, sizeof(u64) * (size_t)ng), "member slots");
+    c->member_cap = ng;
+  }
+  int st = ensure_events(c, 2);
+  if (st != FSGC_OK) return st;
+  st = ensure_slots(c, 1);
+  if (st != FSGC_OK) return st;
+  CK(cudaMemsetAsync(c->d_member, 0, sizeof(u64) * (size_t)ng, c->stream), "slot reset");
+  CK(cudaEventRecord(c->events[0], c->stream), "event");
+  fsgc::CountJob job{mo, g, c->d_slots, 0, 0, false, c->exact_placements, c->d_member, 1};
+  if (any_fits) {
+    st = fsgc::enqueue_count(job, c->stream, &c->launches, c->work);
+    if (st != FSGC_OK) {
+      cudaStreamSynchronize(c->stream);
+      return fail(c, st, "packed count failed (%s)", cudaGetErrorString(cudaGetLastError()));
+    }
+  } else {
+    job.core_type = mo->nodes == 1 ? FSGC_CORE_VERTEX : mo->nodes == 2 ? FSGC_CORE_EDGE
+                   : mo->nodes == 3 ? ((__builtin_popcount(mo->list[1]) == 1) ? FSGC_CORE_WEDGE : FSGC_CORE_TRIANGLE)
+                   : FSGC_CORE_GENERAL;
+  }
+  CK(cudaEventRecord(c->events[1], c->stream), "event");
+  CK(cudaMemcpyAsync(c->h_member, c->d_member, sizeof(u64) * (size_t)ng, cudaMemcpyDeviceToHost, c->stream), "readback");
+  CK(cudaStreamSynchronize(c->stream), "packed count");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->events[0], c->events[1]);
+  for (int i = 0; i < ng; i++) {
+    fsgc_result& r = results[i];
+    memset(&r, 0, sizeof(r));
+    r.core_type = job.core_type;
+    r.device_ms = ms;
+    if (mo->nodes >= 3 && (pn > g->member_n[i] || pm > g->member_m[i])) {
+      r.flags = FSGC_FLAG_PATTERN_TOO_LARGE;
+      continue;
+    }
+    u64 raw;
+    if (job.host_only) raw = (mo->anchorsets == 0) ? (u64)g->member_n[i] : (u64)(g->member_m[i] / 2);
+    else raw = c->h_member[i] / (u64)job.per_member_div;
+    r.raw_total = raw;
+    r.automorphisms = aut;
+    r.count = raw / aut;
+  }
   return FSGC_OK;
 }
 

@@ -44,6 +44,16 @@ enum { IU = 1, IV = 2, IW = 4, IUV = 3, IUW = 5, IVW = 6, IUVW = 7 };
 
 __device__ __forceinline__ u64 nck(int n, int k) { return nck_ref(n, k, c_div); }
 
+// Adds one match's value: into the thread's running sum for an ordinary graph,
+// into the result slot of the match's member graph for a packed graph.
+__device__ __forceinline__ void credit(const GView& g, u64& acc, u64 x, int vertex) {
+  if (g.comp == nullptr) acc += x;
+  else if (x) atomicAdd(g.comp_slots + g.comp[vertex], x);
+}
+__device__ __forceinline__ int relabel_of(const GView& g, int relabel, int vertex) {
+  return g.comp ? (int)g.comp_relabel[g.comp[vertex]] : relabel;
+}
+
 // ------------------------------------------------------------- shared formulas
 // Edge-core formula (src/fringeCount.cu:2030-2049) for an edge (u, v), where
 // u is the endpoint with the larger vertex id and c_uv = |N(u) & N(v)|.
@@ -140,7 +150,7 @@ __global__ void star_kernel(GView g, int t, u64* __restrict__ slot) {
   u64 acc = 0;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x) {
     const int d = g.deg[v];
-    if (d >= t) acc += nck(d, t);
+    if (d >= t) credit(g, acc, nck(d, t), v);
   }
   block_sum_to(acc, slot);
 }
@@ -158,7 +168,7 @@ __global__ void edge_kernel(GView g, EdgeParams p, u64* __restrict__ slot) {
     const int u = max(a, b), v = min(a, b);  // the reference orients by id, v < u
     const int du = g.deg[u], dv = g.deg[v];
     if (!(du > p.lim1 && dv > p.lim1 && du + dv > p.lim2)) continue;  // init_wl_edge pruning
-    acc += edge_formula(du, dv, (int)g.osup[j], p.f_u, p.f_uv, p.f_v);
+    credit(g, acc, edge_formula(du, dv, (int)g.osup[j], p.f_u, p.f_uv, p.f_v), a);
   }
   block_sum_to(acc, slot);
 }
@@ -169,8 +179,16 @@ __global__ void tailed_triangle_kernel(GView g, const u64* __restrict__ vtri2, i
   u64 acc = 0;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x) {
     const u64 t2 = vtri2[v];
-    if (t2) acc += (t2 >> 1) * nck(g.deg[v] - 2, tails);
+    if (t2) credit(g, acc, (t2 >> 1) * nck(g.deg[v] - 2, tails), v);
   }
+  block_sum_to(acc, slot);
+}
+
+// packed graphs: per-member sum of a per-vertex value (6 x triangles from vtri2)
+__global__ void packed_vertex_sum_kernel(GView g, const u64* __restrict__ vals, u64* __restrict__ slot) {
+  u64 acc = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x)
+    credit(g, acc, vals[v], v);
   block_sum_to(acc, slot);
 }
 
@@ -255,9 +273,9 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
           for (int t = 0; t < lc; t++) {
             const int d = __ldg(C + t);
             if (bsearch_has(A, la, d) && bsearch_has(B, lb, d)) {
-              if (p.mode == 1) acc += 1;
-              else acc += nck(g.deg[a] - 3, p.tails) + nck(g.deg[b] - 3, p.tails) + nck(g.deg[c] - 3, p.tails) +
-                          nck(g.deg[d] - 3, p.tails);
+              if (p.mode == 1) credit(g, acc, 1, a);
+              else credit(g, acc, nck(g.deg[a] - 3, p.tails) + nck(g.deg[b] - 3, p.tails) + nck(g.deg[c] - 3, p.tails) +
+                                  nck(g.deg[d] - 3, p.tails), a);
             }
           }
         }
@@ -273,7 +291,8 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
           // supports of edges ab, ac, bc
           const unsigned s_ab = g.osup[j], s_ac = g.osup[aoff + i], s_bc = g.osup[boff + k];
           // sort the three vertices by key descending: u, v, w
-          long long kx[3] = {tri_key(a, dx[0], p.relabel), tri_key(b, dx[1], p.relabel), tri_key(c, dx[2], p.relabel)};
+          const int rl = relabel_of(g, p.relabel, a);
+          long long kx[3] = {tri_key(a, dx[0], rl), tri_key(b, dx[1], rl), tri_key(c, dx[2], rl)};
           int ord[3] = {0, 1, 2};
           if (kx[ord[0]] < kx[ord[1]]) { int t = ord[0]; ord[0] = ord[1]; ord[1] = t; }
           if (kx[ord[1]] < kx[ord[2]]) { int t = ord[1]; ord[1] = ord[2]; ord[2] = t; }
@@ -320,7 +339,9 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
           venn[IV] = dv - (c12 + c23 + (c123 + 2));
           venn[IW] = dw - (c13 + c23 + (c123 + 2));
           venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
-          for (int r = 0; r < p.rot.count; r++) acc += fc3(p.rot.fr[r], venn);
+          u64 t = 0;
+          for (int r = 0; r < p.rot.count; r++) t += fc3(p.rot.fr[r], venn);
+          credit(g, acc, t, a);
         }
       }
       if (found) { i++; k++; }
@@ -405,7 +426,8 @@ __global__ void __launch_bounds__(256) triangle_bitmap_kernel(GView g, TriParams
           const int xv[3] = {a, bi, bj};
           const int dx[3] = {da, di, dj};
           long long kx[3];
-          for (int t = 0; t < 3; t++) kx[t] = tri_key(xv[t], dx[t], p.relabel);
+          const int rl = relabel_of(g, p.relabel, a);
+          for (int t = 0; t < 3; t++) kx[t] = tri_key(xv[t], dx[t], rl);
           int ord[3] = {0, 1, 2};
           if (kx[ord[0]] < kx[ord[1]]) { int t = ord[0]; ord[0] = ord[1]; ord[1] = t; }
           if (kx[ord[1]] < kx[ord[2]]) { int t = ord[1]; ord[1] = ord[2]; ord[2] = t; }
@@ -429,7 +451,9 @@ __global__ void __launch_bounds__(256) triangle_bitmap_kernel(GView g, TriParams
           venn[IV] = dv - (c12 + c23 + (c123 + 2));
           venn[IW] = dw - (c13 + c23 + (c123 + 2));
           venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
-          for (int r = 0; r < p.rot.count; r++) acc += fc3(p.rot.fr[r], venn);
+          u64 t = 0;
+          for (int r = 0; r < p.rot.count; r++) t += fc3(p.rot.fr[r], venn);
+          credit(g, acc, t, a);
         }
       }
     }
@@ -551,10 +575,10 @@ __device__ void block_scan_inplace(int* x, int n, WedgeSmem<BIG>& S) {
 
 template <bool BIG>
 __device__ __forceinline__ void eval_pair(const GView& g, const WedgeParams& p, WedgeSmem<BIG>& S, int lo, int o,
-                                          unsigned C, int dw, int dv, int thres, u64& acc) {
+                                          unsigned C, int dw, int v, int dv, int thres, u64& acc) {
   if (dw >= thres) {
     const bool vw = (S.adjbits[o >> 5] >> (o & 31)) & 1u;
-    acc += (u64)C * wedge_formula(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1);
+    credit(g, acc, (u64)C * wedge_formula(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1), v);
   }
 }
 
@@ -696,14 +720,14 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
             S.cnt[wd] = 0;
             if (BIG) {
               const int w = lo + wd;
-              eval_pair<BIG>(g, p, S, lo, wd, word, g.deg[w], dv, thres, acc);
+              eval_pair<BIG>(g, p, S, lo, wd, word, g.deg[w], v, dv, thres, acc);
             } else {
               const int o0 = 2 * wd;
               const unsigned C0 = word & 0xffffu, C1 = word >> 16;
               const int d0 = C0 ? g.deg[lo + o0] : 0;
               const int d1 = C1 ? g.deg[lo + o0 + 1] : 0;
-              if (C0) eval_pair<BIG>(g, p, S, lo, o0, C0, d0, dv, thres, acc);
-              if (C1) eval_pair<BIG>(g, p, S, lo, o0 + 1, C1, d1, dv, thres, acc);
+              if (C0) eval_pair<BIG>(g, p, S, lo, o0, C0, d0, v, dv, thres, acc);
+              if (C1) eval_pair<BIG>(g, p, S, lo, o0 + 1, C1, d1, v, dv, thres, acc);
             }
           }
         }
@@ -833,14 +857,16 @@ __global__ void wedge_general_kernel(GView g, GWedgeParams p, u64* __restrict__ 
           venn[IV] = dv - (p12 + c23);
           venn[IW] = dw - (c13 + c23 + c123);
           venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
+          u64 t = 0;
           if (tri) {
             venn[IUV]--; venn[IUW]--; venn[IVW]--;
-            for (int r = 0; r < p.rot.count; r++) acc += fc3(p.rot.fr[r], venn);
+            for (int r = 0; r < p.rot.count; r++) t += fc3(p.rot.fr[r], venn);
           } else {
             venn[IU] -= 2; venn[IVW]--;
-            acc += fc3(p.rot.fr[0], venn);
-            if (p.rot.count > 3) acc += fc3(p.rot.fr[3], venn);
+            t += fc3(p.rot.fr[0], venn);
+            if (p.rot.count > 3) t += fc3(p.rot.fr[3], venn);
           }
+          credit(g, acc, t, u);
         }
       }
     }
@@ -1058,7 +1084,8 @@ __device__ u64 gen_level(const GView& g, const GenParams& p, GenWarp& w) {
         venn_general(g, p, w.stack, w.venn[who]);
       }
       __syncwarp();
-      if (ok) acc += p.exact ? placement_sum(p, w.venn[lane]) : placement_sum_reference(p, w.venn[lane]);
+      if (ok) credit(g, acc, p.exact ? placement_sum(p, w.venn[lane]) : placement_sum_reference(p, w.venn[lane]),
+                     w.stack[0]);
       __syncwarp();
     } else {
       while (bal) {
@@ -1197,15 +1224,20 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
   DevGraph& G = *job.g;
   job.host_only = false;
   job.host_value = 0;
+  job.per_member_div = 1;
   if (mo.nodes < 1 || mo.nodes > FSGC_MAX_CORE || mo.anchorsets > 63) return FSGC_EINVAL;
   const int TPB = kTPB;
+  const bool packed = G.ngraphs > 0;
 
   // ---- vertex core (vertexCore, src/fringeCount.cu:2172-2191)
   if (mo.nodes == 1) {
     job.core_type = FSGC_CORE_VERTEX;
+    // single vertex: n; single edge: m/2 (per member graph for packed graphs, on the host)
     if (mo.anchorsets == 0) { job.host_only = true; job.host_value = (u64)G.n; return FSGC_OK; }
     if (mo.fcnt[0] == 1) { job.host_only = true; job.host_value = (u64)(G.m / 2); return FSGC_OK; }
-    star_kernel<<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(G.view(), mo.fcnt[0], job.d_slot);
+    GView gv0 = G.view();
+    gv0.comp_slots = job.d_comp_slots;
+    star_kernel<<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(gv0, mo.fcnt[0], job.d_slot);
     *launches += 1;
     return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
   }
@@ -1213,6 +1245,7 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
   int st = prepare_graph(G, s, launches, work.small);
   if (st != FSGC_OK) return st;
   GView gv = G.view();
+  gv.comp_slots = job.d_comp_slots;
   const long long me = G.m / 2;
 
   // ---- edge core (edgeCore, src/fringeCount.cu:2106-2144)
@@ -1223,9 +1256,18 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
     const int f_u = std::min(f[1], f[2]), f_uv = f[3], f_v = std::max(f[1], f[2]);
     if (f_uv == 1 && (f_u == 0 || f_v == 0)) {
       if (f_u == 0 && f_v == 0) {  // triangle
-        job.host_only = true;
-        job.host_value = (u64)G.triangles;
-        return FSGC_OK;
+        if (!packed) {
+          job.host_only = true;
+          job.host_value = (u64)G.triangles;
+          return FSGC_OK;
+        }
+        // per member: sum of 2 x (triangles at v) over its vertices = 6 x triangles
+        st = ensure_vertex_triangles(G, s, launches);
+        if (st != FSGC_OK) return st;
+        packed_vertex_sum_kernel<<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(gv, G.vtri2, job.d_slot);
+        *launches += 1;
+        job.per_member_div = 6;
+        return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
       }
       st = ensure_vertex_triangles(G, s, launches);
       if (st != FSGC_OK) return st;

@@ -1,6 +1,7 @@
 // Internal types shared by the library's translation units.
 #pragma once
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "fsgc.h"
@@ -25,6 +26,12 @@ struct GView {
   const int* __restrict__ oadj;       // m/2
   const int* __restrict__ osrc;       // m/2
   const unsigned* __restrict__ osup;  // m/2
+  // packed graphs (many member graphs in one CSR): member of each vertex,
+  // the triangle-core relabel gate of each member, and one result slot per
+  // member that kernels add each match into; comp == nullptr for one graph
+  const int* __restrict__ comp;
+  const unsigned char* __restrict__ comp_relabel;
+  u64* comp_slots;
 };
 
 struct DevGraph {
@@ -54,11 +61,18 @@ struct DevGraph {
   // when it fires, vertex ids otherwise
   bool tri_relabel = false;
   size_t bytes = 0;
+  // packed graphs
+  int ngraphs = 0;                 // 0 for an ordinary graph
+  int* comp = nullptr;             // member of each vertex (device)
+  unsigned char* comp_relabel = nullptr;  // per member (device)
+  std::vector<int> member_n;       // per member: vertices, directed entries
+  std::vector<long long> member_m;
 
   GView view() const {
     GView g;
     g.n = n; g.m = m; g.off = off; g.adj = adj; g.deg = deg;
     g.ooff = ooff; g.oadj = oadj; g.osrc = osrc; g.osup = osup;
+    g.comp = comp; g.comp_relabel = comp_relabel; g.comp_slots = nullptr;
     return g;
   }
 };
@@ -95,6 +109,8 @@ struct CountJob {
   u64 host_value;     // used when the result needs no device work (n, m/2, T)
   bool host_only;
   int exact_placements;  // general core: exact placement sum instead of the reference's
+  u64* d_comp_slots;     // packed graphs: per-member result slots (zeroed by the caller)
+  int per_member_div;    // packed graphs: divide each member's total by this on the host (1 = none)
 };
 
 // Launchers over caller-provided device memory (used by noalloc.cu).

@@ -96,6 +96,8 @@ def lib():
             "fsgc_graph_info_get": (I, [P, I, C.POINTER(GraphInfo)]),
             "fsgc_count": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(Result)]),
             "fsgc_count_batch": (I, [P, C.POINTER(Task), I, C.POINTER(Result)]),
+            "fsgc_graph_from_packed_csr": (I, [P, I, I64, P, P, I, P, C.POINTER(C.c_int)]),
+            "fsgc_count_packed": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(Result)]),
             "fsgc_ctx_timer_start": (I, [P]),
             "fsgc_ctx_timer_stop": (I, [P, C.POINTER(C.c_double)]),
             "fsgc_ctx_flush_l2": (I, [P, C.c_size_t]),
@@ -312,6 +314,33 @@ class Context:
         r = Result()
         _check(lib().fsgc_count(self.ptr, gid, C.byref(mo), C.byref(r)), "count", self.ptr)
         return r
+
+    def upload_packed(self, graphs):
+        """Pack member graphs (list of Graph) into one resident graph; returns (gid, ngraphs)."""
+        sizes = np.array([g.n for g in graphs], dtype=np.int64)
+        vstart = np.zeros(len(graphs) + 1, dtype=np.int32)
+        vstart[1:] = np.cumsum(sizes)
+        idx = [np.zeros(1, np.int64)]
+        adj = []
+        base_e = 0
+        for g, v0 in zip(graphs, vstart[:-1]):
+            idx.append(g.nindex[1:] + base_e)
+            adj.append(g.nlist + v0)
+            base_e += g.m
+        packed = Graph(np.concatenate(idx), np.concatenate(adj) if adj else np.zeros(0, np.int32))
+        gid = C.c_int()
+        _check(lib().fsgc_graph_from_packed_csr(self.ptr, packed.n, packed.m, packed.nindex.ctypes.data,
+                                                packed.nlist.ctypes.data, len(graphs), vstart.ctypes.data,
+                                                C.byref(gid)), "graph_from_packed_csr", self.ptr)
+        self._packed_sizes = getattr(self, "_packed_sizes", {})
+        self._packed_sizes[gid.value] = len(graphs)
+        return gid.value
+
+    def count_packed(self, gid, mo):
+        ng = self._packed_sizes[gid]
+        res = (Result * ng)()
+        _check(lib().fsgc_count_packed(self.ptr, gid, C.byref(mo), res), "count_packed", self.ptr)
+        return list(res)
 
     def count_batch(self, tasks):
         """tasks: list of (gid, MatchingOrder)."""

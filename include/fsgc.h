@@ -159,6 +159,16 @@ typedef struct fsgc_graph_info {
 } fsgc_graph_info;
 int fsgc_graph_info_get(fsgc_ctx* ctx, int gid, fsgc_graph_info* out);
 
+/* ---- packed graphs: many member graphs in one resident CSR (the batching-across-
+ *      graphs workload; the reference runs one fringeCount process per graph) ----
+ * Member i owns vertices [vstart[i], vstart[i+1]) (vstart[0] = 0, vstart[ngraphs]
+ * = n); no edge may cross members.  One count covers every member: each
+ * member's result equals a count on that member alone (its own relabel gate,
+ * vertex order and pattern-size check).  results[] has ngraphs entries. */
+int fsgc_graph_from_packed_csr(fsgc_ctx* ctx, int n, int64_t m, const int64_t* nindex, const int32_t* nlist,
+                               int ngraphs, const int32_t* vstart, int* gid);
+int fsgc_count_packed(fsgc_ctx* ctx, int gid, const fsgc_matching_order* mo, fsgc_result* results);
+
 /* ---- counting (replaces `fringeCount <graph> <motif.mo>`, src/fringeCount.cu:2265-2331,
  *      and occurrences(), :2199-2262) ---- */
 
