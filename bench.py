@@ -44,6 +44,19 @@ WORKLOAD = {
     "4clique_3_distinct": (7, [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3), (0, 4), (1, 5), (2, 6)]),
     "edge_5_5": (12, [(0, 1)] + [(0, i) for i in range(2, 7)] + [(1, i) for i in range(7, 12)]),
 }
+# Core shapes of the mixed-pattern workloads (batching and serving): each
+# drawn pattern is one of these cores plus 0-12 fringe vertices, each fringe
+# adjacent to a uniformly random nonempty subset of the core vertices.
+CORE_SHAPES = {
+    "edge": (2, [(0, 1)]),
+    "wedge": (3, [(0, 1), (0, 2)]),
+    "triangle": (3, [(0, 1), (1, 2), (0, 2)]),
+    "4path": (4, [(0, 1), (1, 2), (2, 3)]),
+    "4cycle": (4, [(0, 1), (1, 2), (2, 3), (3, 0)]),
+    "diamond": (4, [(0, 1), (1, 2), (2, 3), (3, 0), (0, 2)]),
+    "4clique": (4, [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]),
+    "5cycle": (5, [(0, 1), (1, 2), (2, 3), (3, 4), (4, 0)]),
+}
 RMAT = dict(scale=22, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=20251203)
 METRIC = "pattern counts/s (RMAT-22, 8 single patterns)"
 UNIT = "patterns/s"
@@ -125,6 +138,41 @@ def workload_graph(scale=None):
 def matching_orders(names=None):
     import fsgc
     return [(name, fsgc.preprocess(n, e)) for name, (n, e) in WORKLOAD.items() if not names or name in names]
+
+
+def draw_patterns(count, seed, max_fringes=12, max_core=6):
+    """Seeded mixed patterns: a core shape, then 0..max_fringes fringe vertices
+    each joined to a uniformly random nonempty subset of the core vertices.
+    Draws whose decomposition is refused (a core of more than six vertices) or
+    whose decomposed core has more than max_core vertices are drawn again.
+    Returns [(name, MatchingOrder)].
+
+    max_core=3 keeps the vertex, edge, wedge and triangle cores.  Cores of four
+    or more vertices sum, per core match, the reference's fringe-placement
+    enumeration (src/fringeCount.cu:408-486), whose cost grows exponentially
+    with the number of anchor sets: with five or more anchor sets the oracle
+    needs more than 20 s on a 256-vertex RMAT graph, and the match count grows
+    by orders of magnitude per RMAT scale."""
+    import fsgc
+    rng = np.random.default_rng(seed)
+    names = list(CORE_SHAPES)
+    out = []
+    while len(out) < count:
+        shape = names[int(rng.integers(len(names)))]
+        k, core = CORE_SHAPES[shape]
+        nf = int(rng.integers(0, max_fringes + 1))
+        edges = list(core)
+        for i in range(nf):
+            sub = int(rng.integers(1, 1 << k))
+            edges += [(j, k + i) for j in range(k) if sub >> j & 1]
+        try:
+            mo = fsgc.preprocess(k + nf, edges)
+        except fsgc.FsgcError:
+            continue
+        if mo.nodes > max_core:
+            continue
+        out.append((f"{shape}+{nf}#{len(out)}", mo))
+    return out
 
 
 def wedge_bytes(g):
@@ -278,8 +326,153 @@ def cpu_sample(g, mos, budget_s, threads):
     return est, samples
 
 
+def mixed_graphs(count, nmax, seed):
+    """Chung-Lu member graphs of uneven size: n log-uniform in [1000, nmax],
+    average degree uniform in [4, 64], exponent uniform in [2.1, 2.8]."""
+    import fsgc
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(round(float(np.exp(rng.uniform(np.log(1000), np.log(nmax))))))
+        d, e = float(rng.uniform(4, 64)), float(rng.uniform(2.1, 2.8))
+        out.append(fsgc.gen_chung_lu(n, d, e, seed * 1000003 + i))
+    return out
+
+
+def run_packed(args):
+    """Batching across graphs: every member graph counted with the same
+    patterns, (a) packed -- one count per pattern covering all members -- and
+    (b) one fsgc_count per (graph, pattern).  Both wall-clock, results read
+    back; every per-(graph, pattern) count must agree."""
+    import fsgc
+    ctx = fsgc.Context(0)
+    t = time.time()
+    graphs = mixed_graphs(args.graphs, args.nmax, 20251204)
+    gen_s = time.time() - t
+    pats = draw_patterns(8, 20251205, max_core=3)
+    pid = ctx.upload_packed(graphs)
+    ctx.prepare(pid)
+    gids = [ctx.upload(g) for g in graphs]
+    for gid in gids:
+        ctx.prepare(gid)
+    nq = len(graphs) * len(pats)
+    launches0 = ctx.launches
+    for _ in range(args.warmup):
+        packed = [ctx.count_packed(pid, mo) for _, mo in pats]
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        packed = [ctx.count_packed(pid, mo) for _, mo in pats]
+    t_packed = (time.perf_counter() - t0) / args.steps
+    launches = (ctx.launches - launches0) // (args.steps + args.warmup)
+    single = None
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        single = [[ctx.count(gid, mo) for gid in gids] for _, mo in pats]
+    t_single = (time.perf_counter() - t0) / max(1, args.steps // 2)
+    for pi in range(len(pats)):
+        for gi in range(len(graphs)):
+            a, b = packed[pi][gi], single[pi][gi]
+            assert (a.count, a.raw_total, a.flags) == (b.count, b.raw_total, b.flags), (pi, gi)
+    line = {"metric": "queries/s, batched across graphs (packed CSR, one count per pattern)",
+            "value": nq / t_packed, "unit": "queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_packed * 1000, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64", "data": "synthetic",
+            "config": {"workload": f"{len(graphs)} Chung-Lu graphs, n log-uniform [1000, {args.nmax}], avg degree "
+                                   "U[4,64], exponent U[2.1,2.8], packed into one CSR; 8 mixed patterns",
+                       "n_total": int(sum(g.n for g in graphs)), "m_total": int(sum(g.m for g in graphs)),
+                       "patterns": [n for n, _ in pats], "gen_s": round(gen_s, 1)},
+            "one_query_per_launch": {"value": nq / t_single, "unit": "queries/s", "ms_per_step": t_single * 1000},
+            "batched_over_single": (nq / t_packed) / (nq / t_single),
+            "gpu_launches": launches, "exact": "all per-(graph, pattern) counts equal"}
+    print(json.dumps(line))
+    ctx.close()
+
+
+def run_serve(args):
+    """Serving: resident RMAT graphs, Poisson arrivals of (random graph, random
+    mixed pattern) queries into fsgc_server_*, p50/p99 latency and queries/s,
+    then the same queries as one closed burst with continuous batching and with
+    one query per launch (one lane, batches of one).  Every served count is
+    compared with a direct count of the same query."""
+    import fsgc
+    ctx = fsgc.Context(0)
+    scales = [int(x) for x in args.serve_scales.split(",")]
+    t = time.time()
+    graphs = [fsgc.gen_rmat(sc, RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], RMAT["seed"] + sc)
+              for sc in scales]
+    gen_s = time.time() - t
+    gids = [ctx.upload(g) for g in graphs]
+    pats = draw_patterns(64, 20251206, max_core=3)
+    rng = np.random.default_rng(20251207)
+    nq = args.queries
+    qs = [(int(rng.integers(len(gids))), int(rng.integers(len(pats)))) for _ in range(nq)]
+    gaps = rng.exponential(1.0 / args.rate, nq)
+    # pattern divisors and per-graph structures are built once, before serving
+    direct = {}
+    t = time.time()
+    for gi, pi in sorted(set(qs)):
+        direct[(gi, pi)] = ctx.count(gids[gi], pats[pi][1])
+    print(f"serve: {len(direct)} direct counts in {time.time() - t:.1f} s", file=sys.stderr, flush=True)
+    budget = int(args.budget_gb * (1 << 30))
+
+    def serve(lanes, max_batch, arrivals):
+        with fsgc.Server(ctx, budget, lanes=lanes, max_batch=max_batch) as srv:
+            for gid in gids:
+                srv.add_graph(gid)
+            tickets = []
+            t0 = time.perf_counter()
+            at = 0.0
+            for k, (gi, pi) in enumerate(qs):
+                if arrivals:
+                    at += gaps[k]
+                    d = t0 + at - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                tickets.append(srv.submit(gids[gi], pats[pi][1]))
+            res = [srv.wait(tk, timeout_s=3600) for tk in tickets]
+            st = srv.stats()
+            wall = time.perf_counter() - t0
+        for (gi, pi), (r, _) in zip(qs, res):
+            d = direct[(gi, pi)]
+            assert (r.count, r.raw_total) == (d.count, d.raw_total), (gi, pi)
+        return {"queries_per_s": st.queries_per_s, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
+                "rounds": int(st.rounds), "wall_s": wall}
+
+    launches0 = ctx.launches
+    poisson = serve(args.lanes, 64, True)
+    launches = ctx.launches - launches0
+    print(f"serve: poisson {poisson}", file=sys.stderr, flush=True)
+    burst = serve(args.lanes, 64, False)
+    print(f"serve: burst {burst}", file=sys.stderr, flush=True)
+    single = serve(1, 1, False)
+    line = {"metric": f"served queries/s at Poisson {args.rate:g}/s offered (p50/p99 latency beside)",
+            "value": poisson["queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": poisson["wall_s"] * 1000, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": f"{len(graphs)} resident RMAT graphs (scales {scales}, edge factor 16), "
+                                   f"{nq} queries, uniform graph x 64 mixed patterns",
+                       "lanes": args.lanes, "budget_gb": args.budget_gb, "gen_s": round(gen_s, 1)},
+            "p50_ms": poisson["p50_ms"], "p99_ms": poisson["p99_ms"], "poisson": poisson,
+            "burst_batched": burst, "burst_one_query_per_launch": single,
+            "batched_over_single": burst["queries_per_s"] / max(single["queries_per_s"], 1e-12),
+            "gpu_launches": launches, "exact": "every served count equals the direct count"}
+    print(json.dumps(line))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="rmat22", choices=["rmat22", "packed", "serve"],
+                    help="rmat22: the eight-pattern RMAT-22 step (default); packed: batching across graphs; "
+                         "serve: the serving loop")
+    ap.add_argument("--graphs", type=int, default=256, help="packed: member graphs")
+    ap.add_argument("--nmax", type=int, default=50000, help="packed: largest member size")
+    ap.add_argument("--serve-scales", default="10,11,12,13,14,15,16,17", help="serve: RMAT scales")
+    ap.add_argument("--queries", type=int, default=2000, help="serve: queries")
+    ap.add_argument("--rate", type=float, default=500.0, help="serve: Poisson arrivals per second")
+    ap.add_argument("--lanes", type=int, default=4, help="serve: lanes")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="serve: work-arena budget")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
@@ -316,6 +509,14 @@ def main():
                                            json.dumps(samples) + "; t_scan + (t - t_scan) x stride"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+    if args.workload == "packed":
+        if rank == 0:
+            run_packed(args)
+        return
+    if args.workload == "serve":
+        if rank == 0:
+            run_serve(args)
         return
     if world > 1:
         import torch

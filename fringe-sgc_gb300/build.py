@@ -61,7 +61,7 @@ def build(verbose=False):
         for out in ex.map(_run, jobs):
             logs.append(out)
     if _stale(LIB, objs):
-        _run([NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lgomp"])
+        _run([NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lgomp", "-lpthread"])
     clis = []
     for f in sorted(os.listdir(os.path.join(HERE, "cli"))):
         if not f.endswith(".cpp"):

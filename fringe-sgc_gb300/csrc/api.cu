@@ -43,6 +43,21 @@ struct fsgc_ctx {
   size_t flush_bytes = 0;
 };
 
+struct fsgc_lane {
+  fsgc_ctx* ctx = nullptr;
+  cudaStream_t stream = nullptr;
+  fsgc::DevWork work;
+  u64* d_slots = nullptr;
+  u64* h_slots = nullptr;
+  int cap = 0;
+  std::vector<cudaEvent_t> events;  // blocking-sync: waiting threads sleep
+  std::vector<fsgc_task> tasks;     // the submission in flight (jobs point here)
+  std::vector<fsgc::CountJob> jobs;
+  std::vector<u64> aut;
+  std::vector<fsgc_result> res;
+  int pending = 0;
+};
+
 namespace {
 
 std::mutex g_init_mu;
@@ -238,32 +253,35 @@ DevGraph* find_graph(fsgc_ctx* c, int gid) {
   return it == c->graphs.end() ? nullptr : it->second;
 }
 
-int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
-  if (nt <= 0) return FSGC_OK;
-  int st = ensure_slots(c, nt);
-  if (st != FSGC_OK) return st;
-  st = ensure_events(c, (size_t)nt + 1);
-  if (st != FSGC_OK) return st;
-  std::vector<u64> aut((size_t)nt, 1);
-  std::vector<fsgc::CountJob> jobs((size_t)nt);
+// Host checks of a batch and the divisors of its patterns (context lock held).
+int plan_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, std::vector<u64>& aut) {
+  aut.assign((size_t)nt, 1);
   for (int t = 0; t < nt; t++) {
     const fsgc_matching_order& mo = tasks[t].mo;
-    memset(&res[t], 0, sizeof(fsgc_result));
     if (!mo_valid(mo)) return fail(c, FSGC_EINVAL, "task %d: malformed matching order", t);
     DevGraph* g = find_graph(c, tasks[t].gid);
     if (!g) return fail(c, FSGC_ENOTFOUND, "task %d: unknown graph %d", t, tasks[t].gid);
     if (g->ngraphs > 0) return fail(c, FSGC_EINVAL, "task %d: graph %d is packed; use fsgc_count_packed", t, tasks[t].gid);
     if (mo.nodes >= 3 && !pattern_too_large(mo, *g)) {
-      st = automorphisms(c, mo, &aut[t]);
+      const int st = automorphisms(c, mo, &aut[(size_t)t]);
       if (st != FSGC_OK) return st;
     }
   }
-  CK(cudaMemsetAsync(c->d_slots, 0, sizeof(u64) * (size_t)nt, c->stream), "slot reset");
-  CK(cudaEventRecord(c->events[0], c->stream), "event");
+  return FSGC_OK;
+}
+
+// Enqueues a planned batch on `s`: slot reset, each task's kernels between
+// events ev[t] and ev[t+1], and the read-back of the raw totals into h_slots.
+int enqueue_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, cudaStream_t s, fsgc::DevWork& work, u64* d_slots,
+                  u64* h_slots, const cudaEvent_t* ev, std::vector<fsgc::CountJob>& jobs, fsgc_result* res) {
+  jobs.assign((size_t)nt, fsgc::CountJob{});
+  CK(cudaMemsetAsync(d_slots, 0, sizeof(u64) * (size_t)nt, s), "slot reset");
+  CK(cudaEventRecord(ev[0], s), "event");
   for (int t = 0; t < nt; t++) {
     const fsgc_matching_order& mo = tasks[t].mo;
     DevGraph* g = find_graph(c, tasks[t].gid);
-    jobs[t] = fsgc::CountJob{&tasks[t].mo, g, c->d_slots + t, 0, 0, false, c->exact_placements, nullptr, 1};
+    memset(&res[t], 0, sizeof(fsgc_result));
+    jobs[t] = fsgc::CountJob{&tasks[t].mo, g, d_slots + t, 0, 0, false, c->exact_placements, nullptr, 1};
     if (pattern_too_large(mo, *g)) {
       jobs[t].host_only = true;
       jobs[t].host_value = 0;
@@ -271,27 +289,50 @@ int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
                                           : FSGC_CORE_GENERAL;
       res[t].flags |= FSGC_FLAG_PATTERN_TOO_LARGE;
     } else {
-      st = fsgc::enqueue_count(jobs[t], c->stream, &c->launches, c->work);
+      const int st = fsgc::enqueue_count(jobs[t], s, &c->launches, work);
       if (st != FSGC_OK) {
-        cudaStreamSynchronize(c->stream);
+        cudaStreamSynchronize(s);
         return fail(c, st, "task %d: count failed (%s)", t, cudaGetErrorString(cudaGetLastError()));
       }
     }
-    CK(cudaEventRecord(c->events[t + 1], c->stream), "event");
+    CK(cudaEventRecord(ev[t + 1], s), "event");
   }
-  CK(cudaMemcpyAsync(c->h_slots, c->d_slots, sizeof(u64) * (size_t)nt, cudaMemcpyDeviceToHost, c->stream), "readback");
-  CK(cudaStreamSynchronize(c->stream), "count");
+  CK(cudaMemcpyAsync(h_slots, d_slots, sizeof(u64) * (size_t)nt, cudaMemcpyDeviceToHost, s), "readback");
+  return FSGC_OK;
+}
+
+// Results of a finished batch (its stream has completed).
+void finish_tasks(int nt, const std::vector<fsgc::CountJob>& jobs, const std::vector<u64>& aut, const u64* h_slots,
+                  const cudaEvent_t* ev, fsgc_result* res) {
   for (int t = 0; t < nt; t++) {
-    const u64 raw = jobs[t].host_only ? jobs[t].host_value : c->h_slots[t];
+    const u64 raw = jobs[t].host_only ? jobs[t].host_value : h_slots[t];
+    const bool too_large = (res[t].flags & FSGC_FLAG_PATTERN_TOO_LARGE) != 0;
     res[t].raw_total = raw;
     // no divisor is computed when the pattern does not fit the graph
-    res[t].automorphisms = (res[t].flags & FSGC_FLAG_PATTERN_TOO_LARGE) ? 0 : aut[t];
-    res[t].count = (res[t].flags & FSGC_FLAG_PATTERN_TOO_LARGE) ? 0 : raw / aut[t];
+    res[t].automorphisms = too_large ? 0 : aut[t];
+    res[t].count = too_large ? 0 : raw / aut[t];
     res[t].core_type = jobs[t].core_type;
     float ms = 0;
-    cudaEventElapsedTime(&ms, c->events[t], c->events[t + 1]);
+    cudaEventElapsedTime(&ms, ev[t], ev[t + 1]);
     res[t].device_ms = ms;
   }
+}
+
+int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
+  if (nt <= 0) return FSGC_OK;
+  for (int t = 0; t < nt; t++) memset(&res[t], 0, sizeof(fsgc_result));
+  int st = ensure_slots(c, nt);
+  if (st != FSGC_OK) return st;
+  st = ensure_events(c, (size_t)nt + 1);
+  if (st != FSGC_OK) return st;
+  std::vector<u64> aut;
+  st = plan_tasks(c, tasks, nt, aut);
+  if (st != FSGC_OK) return st;
+  std::vector<fsgc::CountJob> jobs;
+  st = enqueue_tasks(c, tasks, nt, c->stream, c->work, c->d_slots, c->h_slots, c->events.data(), jobs, res);
+  if (st != FSGC_OK) return st;
+  CK(cudaStreamSynchronize(c->stream), "count");
+  finish_tasks(nt, jobs, aut, c->h_slots, c->events.data(), res);
   return FSGC_OK;
 }
 
@@ -638,6 +679,139 @@ int fsgc_count_batch(fsgc_ctx* c, const fsgc_task* tasks, int ntasks, fsgc_resul
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   return count_tasks(c, tasks, ntasks, results);
+}
+
+// ---- lanes: asynchronous counts on their own streams.  The context lock is
+// held while a submission is checked and enqueued, never while it runs, so
+// submissions on different lanes overlap on the device.
+int fsgc_lane_create(fsgc_ctx* c, fsgc_lane** out) {
+  if (!c || !out) return FSGC_EINVAL;
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  fsgc_lane* L = new fsgc_lane();
+  L->ctx = c;
+  cudaError_t e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&L->work.small, 32 * sizeof(u64));
+  if (e == cudaSuccess) e = cudaMemsetAsync(L->work.small, 0, 32 * sizeof(u64), L->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    fsgc_lane_destroy(L);
+    return cuda_fail(c, e, "lane creation");
+  }
+  *out = L;
+  return FSGC_OK;
+}
+
+void fsgc_lane_destroy(fsgc_lane* L) {
+  if (!L) return;
+  cudaSetDevice(L->ctx->device);
+  if (L->stream) cudaStreamSynchronize(L->stream);
+  for (auto e : L->events) cudaEventDestroy(e);
+  cudaFree(L->work.small);
+  cudaFree(L->work.tri.ptr);
+  cudaFree(L->d_slots);
+  cudaFreeHost(L->h_slots);
+  if (L->stream) cudaStreamDestroy(L->stream);
+  delete L;
+}
+
+int fsgc_lane_submit(fsgc_lane* L, const fsgc_task* tasks, int ntasks) {
+  if (!L || ntasks < 1 || !tasks) return FSGC_EINVAL;
+  fsgc_ctx* c = L->ctx;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  if (L->pending > 0) return fail(c, FSGC_EBUSY, "lane has a submission in flight");
+  L->tasks.assign(tasks, tasks + ntasks);
+  int st = plan_tasks(c, L->tasks.data(), ntasks, L->aut);
+  if (st != FSGC_OK) return st;
+  // one-time per-graph structures are built on the context's stream before
+  // any lane reads them
+  for (int t = 0; t < ntasks; t++) {
+    DevGraph* g = find_graph(c, L->tasks[t].gid);
+    if (pattern_too_large(L->tasks[t].mo, *g)) continue;
+    st = fsgc::prepare_for_count(L->tasks[t].mo, *g, c->stream, &c->launches, c->work);
+    if (st != FSGC_OK) return fail(c, st, "graph preparation failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  if (ntasks > L->cap) {
+    cudaStreamSynchronize(L->stream);
+    cudaFree(L->d_slots);
+    cudaFreeHost(L->h_slots);
+    L->d_slots = nullptr;
+    L->h_slots = nullptr;
+    L->cap = 0;
+    CK(cudaMalloc((void**)&L->d_slots, sizeof(u64) * (size_t)ntasks), "lane slots");
+    CK(cudaMallocHost((void**)&L->h_slots, sizeof(u64) * (size_t)ntasks), "lane slots");
+    L->cap = ntasks;
+  }
+  while (L->events.size() < (size_t)ntasks + 1) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventBlockingSync), "event creation");
+    L->events.push_back(e);
+  }
+  L->res.assign((size_t)ntasks, fsgc_result{});
+  st = enqueue_tasks(c, L->tasks.data(), ntasks, L->stream, L->work, L->d_slots, L->h_slots, L->events.data(),
+                     L->jobs, L->res.data());
+  if (st != FSGC_OK) return st;
+  CK(cudaEventRecord(L->events[(size_t)ntasks], L->stream), "event");
+  L->pending = ntasks;
+  return FSGC_OK;
+}
+
+int fsgc_lane_wait(fsgc_lane* L, fsgc_result* results) {
+  if (!L) return FSGC_EINVAL;
+  if (L->pending <= 0) return FSGC_ENOTFOUND;
+  cudaSetDevice(L->ctx->device);
+  // the host thread sleeps until the lane's last event (blocking-sync event)
+  const cudaError_t e = cudaEventSynchronize(L->events[(size_t)L->pending]);
+  const int nt = L->pending;
+  L->pending = 0;
+  if (e != cudaSuccess) {
+    std::lock_guard<std::mutex> lk(L->ctx->mu);
+    return cuda_fail(L->ctx, e, "lane count");
+  }
+  finish_tasks(nt, L->jobs, L->aut, L->h_slots, L->events.data(), L->res.data());
+  if (results) memcpy(results, L->res.data(), sizeof(fsgc_result) * (size_t)nt);
+  return FSGC_OK;
+}
+
+int fsgc_lane_query(fsgc_lane* L) {
+  if (!L) return FSGC_EINVAL;
+  if (L->pending <= 0) return FSGC_ENOTFOUND;
+  const cudaError_t e = cudaEventQuery(L->events[(size_t)L->pending]);
+  if (e == cudaErrorNotReady) return FSGC_EBUSY;
+  return e == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+
+size_t fsgc_lane_scratch_bytes(const fsgc_lane* L) { return L ? L->work.tri.bytes : 0; }
+
+int fsgc_lane_trim(fsgc_lane* L) {
+  if (!L) return FSGC_EINVAL;
+  if (L->pending > 0) return FSGC_EBUSY;
+  if (L->work.tri.ptr) {
+    cudaSetDevice(L->ctx->device);
+    cudaFreeAsync(L->work.tri.ptr, L->stream);
+    L->work.tri.ptr = nullptr;
+    L->work.tri.bytes = 0;
+  }
+  return FSGC_OK;
+}
+
+int fsgc_task_footprint(fsgc_ctx* c, const fsgc_task* task, size_t* bytes) {
+  if (!c || !task || !bytes) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  *bytes = 0;
+  if (!mo_valid(task->mo)) return fail(c, FSGC_EINVAL, "malformed matching order");
+  DevGraph* g = find_graph(c, task->gid);
+  if (!g) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", task->gid);
+  if (g->ngraphs > 0) return fail(c, FSGC_EINVAL, "graph %d is packed", task->gid);
+  if (pattern_too_large(task->mo, *g) || task->mo.nodes < 2) return FSGC_OK;
+  const int st = fsgc::prepare_graph(*g, c->stream, &c->launches, c->work.small);
+  if (st != FSGC_OK) return fail(c, st, "graph preparation failed: %s", cudaGetErrorString(cudaGetLastError()));
+  *bytes = fsgc::count_scratch_bytes(task->mo, *g);
+  return FSGC_OK;
 }
 
 // Host evaluation of the device binomial (same magic-number division) so that

@@ -791,14 +791,23 @@ __global__ void wedge_general_kernel(GView g, GWedgeParams p, u64* __restrict__ 
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   u64 acc = 0;
-  for (int u = wid; u < g.n; u += nw) {
+  // one warp per list entry (u, v): a hub centre's pairs spread over as many
+  // warps as it has neighbours
+  for (long long j = wid; j < g.m; j += nw) {
+    int lo = 0, hi = g.n;  // u = the last vertex with off[u] <= j
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (g.off[mid] <= j) lo = mid;
+      else hi = mid;
+    }
+    const int u = lo;
     const int du = g.deg[u];
     if (du < p.sum1) continue;
     const long long ub = g.off[u];
     const int* Nu = g.adj + ub;
     const int th1u = max(p.sum1, p.sum2 - du);
-    for (int iv = 0; iv < du; iv++) {
-      const int v = __ldg(Nu + iv);
+    {
+      const int v = __ldg(g.adj + j);
       const int dv = g.deg[v];
       if (dv < th1u) continue;  // init_wl_wedge
       const int* Nv = g.adj + g.off[v];
@@ -1201,23 +1210,106 @@ int ensure_chunk_table(DevGraph& G, cudaStream_t s, uint64_t* launches, u64* d_s
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }
 
+// Stream-ordered, so that growing one stream's arena neither waits for nor
+// stalls work queued on other streams.
 int ensure_plain_scratch(Scratch& sc, size_t need, cudaStream_t s) {
   if (sc.bytes >= need) return FSGC_OK;
   if (sc.ptr) {
-    cudaStreamSynchronize(s);
-    cudaFree(sc.ptr);
+    cudaFreeAsync(sc.ptr, s);
     sc.ptr = nullptr;
     sc.bytes = 0;
   }
-  if (cudaMalloc(&sc.ptr, need) != cudaSuccess) {
+  if (cudaMallocAsync(&sc.ptr, need, s) != cudaSuccess) {
     cudaGetLastError();
+    sc.ptr = nullptr;
     return FSGC_ENOMEM;
   }
   sc.bytes = need;
   return FSGC_OK;
 }
 
+// Triangle bitmap kernel geometry: rows of ceil(deg/32) words per out-neighbour
+// of the block's vertex, one arena of max_bitmap_words per block, at most 8 GiB.
+void triangle_bitmap_geometry(const DevGraph& G, long long* per_block, int* blocks) {
+  *per_block = std::max(1LL, G.max_bitmap_words);
+  const size_t budget = (size_t)8 << 30;
+  *blocks = (int)std::max<size_t>(
+      1, std::min<size_t>((size_t)sm_count() * 4, budget / (sizeof(unsigned) * (size_t)*per_block)));
+}
+
+bool triangle_uses_bitmaps(const fsgc_matching_order& mo, const DevGraph& G, int mode) {
+  const size_t smem = (size_t)3 * sizeof(int) * (size_t)std::max(1LL, G.max_outdeg);
+  return mode == 0 && smem <= (size_t)96 * 1024 && G.m / 2 > 0;
+}
+
 }  // namespace
+
+// What a count of `mo` on `G` needs beyond the resident graph.  The shape
+// tests repeat enqueue_count's dispatch.
+namespace {
+struct Needs {
+  bool chunk_table = false;  // wedge core with a fringe-free centre
+  bool vertex_triangles = false;
+  size_t scratch = 0;        // arena bytes (hub cursors, triangle bitmaps)
+};
+
+Needs needs_of(const fsgc_matching_order& mo, const DevGraph& G) {
+  Needs nd;
+  if (mo.nodes < 2 || mo.nodes > FSGC_MAX_CORE) return nd;
+  if (mo.nodes == 2) {
+    int f[4] = {0, 0, 0, 0};
+    for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 3] = mo.fcnt[i];
+    const int f_u = std::min(f[1], f[2]), f_uv = f[3], f_v = std::max(f[1], f[2]);
+    if (f_uv == 1 && (f_u == 0 || f_v == 0)) nd.vertex_triangles = !(f_u == 0 && f_v == 0) || G.ngraphs > 0;
+    return nd;
+  }
+  if (mo.nodes > 3) return nd;
+  int f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 7] = mo.fcnt[i];
+  if (__builtin_popcount(mo.list[1]) == 1) {
+    if (mo.list[1] == 2) {
+      std::swap(f[IU], f[IV]);
+      std::swap(f[IUW], f[IVW]);
+    }
+    if (f[IUVW] == 0 && f[IUV] == 0 && f[IUW] == 0 && f[IU] == 0) {
+      nd.chunk_table = true;
+      if (G.maxdeg > kWDvMax) {
+        const long long gs = G.maxdeg;
+        nd.scratch = (size_t)sm_count() * ((size_t)2 * gs * sizeof(long long) + (size_t)(gs + 1) * sizeof(int));
+      }
+    }
+    return nd;
+  }
+  const bool clique = (f[IUVW] == 1) && (f[IUV] + f[IUW] + f[IVW] == 0) &&
+                      ((f[IU] == 0) + (f[IV] == 0) + (f[IW] == 0) >= 2);
+  if (triangle_uses_bitmaps(mo, G, clique ? 1 : 0)) {
+    long long per_block;
+    int blocks;
+    triangle_bitmap_geometry(G, &per_block, &blocks);
+    nd.scratch = sizeof(unsigned) * (size_t)per_block * (size_t)blocks;
+  }
+  return nd;
+}
+}  // namespace
+
+size_t count_scratch_bytes(const fsgc_matching_order& mo, const DevGraph& G) { return needs_of(mo, G).scratch; }
+
+int prepare_for_count(const fsgc_matching_order& mo, DevGraph& G, cudaStream_t s, uint64_t* launches,
+                      DevWork& work) {
+  if (mo.nodes < 2) return FSGC_OK;
+  int st = prepare_graph(G, s, launches, work.small);
+  if (st != FSGC_OK) return st;
+  const Needs nd = needs_of(mo, G);
+  if (nd.chunk_table) {
+    st = ensure_chunk_table(G, s, launches, work.small + 9);
+    if (st != FSGC_OK) return st;
+  }
+  if (nd.vertex_triangles) {
+    st = ensure_vertex_triangles(G, s, launches);
+    if (st != FSGC_OK) return st;
+  }
+  return cudaStreamSynchronize(s) == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
 
 int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work) {
   const fsgc_matching_order& mo = *job.mo;
@@ -1334,7 +1426,7 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
     GWedgeParams gp;
     gp.min_u = min_u; gp.lim = lim; gp.sum1 = sum1; gp.sum2 = sum2; gp.sum3 = sum3;
     rotations3(f, true, gp.rot);
-    wedge_general_kernel<<<grid_for((long long)G.n * 32, TPB, 8), TPB, 0, s>>>(gv, gp, job.d_slot);
+    wedge_general_kernel<<<grid_for(G.m * 32, TPB, 8), TPB, 0, s>>>(gv, gp, job.d_slot);
     *launches += 1;
     return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
   }
@@ -1358,12 +1450,10 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
     rotations3(f, false, tp.rot);
     if (me == 0) return FSGC_OK;
     const size_t smem = (size_t)3 * sizeof(int) * (size_t)std::max(1, tp.kmax);
-    if (tp.mode == 0 && smem <= (size_t)96 * 1024) {
-      // bitmap kernel: rows of ceil(deg/32) words per out-neighbour, per block
-      const long long per_block = std::max(1LL, G.max_bitmap_words);
-      int blocks = sm_count() * 4;
-      const size_t budget = (size_t)8 << 30;
-      blocks = (int)std::max<size_t>(1, std::min<size_t>((size_t)blocks, budget / (sizeof(unsigned) * (size_t)per_block)));
+    if (triangle_uses_bitmaps(mo, G, tp.mode)) {
+      long long per_block;
+      int blocks;
+      triangle_bitmap_geometry(G, &per_block, &blocks);
       const size_t need = sizeof(unsigned) * (size_t)per_block * (size_t)blocks;
       st = ensure_plain_scratch(work.tri, need, s);
       if (st != FSGC_OK) return st;

@@ -123,5 +123,12 @@ int wedge_small_max_degree();
 
 // Enqueue the kernels that add the raw total of `mo` on `g` into *d_slot.
 int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work);
+// Builds, on `s` and synchronously, every per-graph structure a count of `mo`
+// would otherwise build on first use, so that counts enqueued afterwards on
+// other streams only read the graph.
+int prepare_for_count(const fsgc_matching_order& mo, DevGraph& g, cudaStream_t s, uint64_t* launches,
+                      DevWork& work);
+// Scratch-arena bytes a count of `mo` on the prepared graph `g` grows to.
+size_t count_scratch_bytes(const fsgc_matching_order& mo, const DevGraph& g);
 
 }  // namespace fsgc

@@ -1,0 +1,310 @@
+// Serving loop: resident graphs, count queries admitted by memory footprint,
+// continuous batching over lanes.
+//
+// The reference has no serving mode (one fringeCount process per query).  Here
+// each of the server's lanes (a CUDA stream of the context with its own work
+// arena, see fsgc_lane_*) has a worker thread.  Queries arrive from any thread
+// through fsgc_server_submit and wait in arrival order.  A free worker admits
+// queries from the head of the queue -- its share of what is waiting, at most
+// max_batch -- while the lanes' work arenas, grown to this batch's need, stay
+// within the memory budget, submits them to its lane and sleeps until they
+// finish.  Meanwhile the other workers admit and submit what arrives, so work
+// from different batches overlaps on the device and no query waits for a
+// batch that was already running when it arrived.  A batch that fails is
+// re-run one query at a time, so that a bad query fails alone.  Latency is
+// submission to completion.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "fsgc.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Query {
+  uint64_t ticket;
+  int gid;
+  fsgc_matching_order mo;
+  size_t footprint;
+  Clock::time_point submitted;
+  bool done = false;
+  int status = FSGC_OK;
+  fsgc_result result{};
+  double latency_ms = 0;
+};
+
+struct LaneSlot {
+  fsgc_lane* lane = nullptr;
+  size_t held = 0;  // arena bytes this lane holds or has reserved
+  bool busy = false;
+};
+
+}  // namespace
+
+struct fsgc_server {
+  fsgc_ctx* ctx = nullptr;
+  size_t budget = 0;
+  size_t held_total = 0;  // sum of LaneSlot::held
+  int max_batch = 64;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<uint64_t> waiting;  // admission queue (submission order)
+  std::map<uint64_t, Query> queries;
+  uint64_t next_ticket = 1;
+  bool stop = false;
+  std::vector<LaneSlot> lanes;
+  std::vector<std::thread> workers;
+  std::map<int, int> graphs;  // registered graph ids
+  // statistics
+  std::vector<double> latencies;
+  uint64_t completed = 0, rounds = 0;
+  Clock::time_point first_submit, last_done;
+  bool any = false;
+};
+
+namespace {
+
+// Takes this lane's batch from the head of the queue (server lock held).
+// Returns false when nothing fits the budget now.
+bool admit(fsgc_server* s, LaneSlot& ls, std::vector<uint64_t>& batch) {
+  int idle = 0;
+  for (const LaneSlot& l : s->lanes) idle += l.busy ? 0 : 1;
+  const size_t share = (s->waiting.size() + (size_t)std::max(1, idle) - 1) / (size_t)std::max(1, idle);
+  const size_t take = std::min<size_t>((size_t)s->max_batch, std::max<size_t>(1, share));
+  size_t need = 0;
+  while (!s->waiting.empty() && batch.size() < take) {
+    const Query& q = s->queries[s->waiting.front()];
+    const size_t nneed = std::max(need, q.footprint);
+    const size_t mine = std::max(ls.held, nneed);
+    if (s->held_total - ls.held + mine > s->budget) break;
+    need = nneed;
+    batch.push_back(q.ticket);
+    s->waiting.pop_front();
+  }
+  if (batch.empty()) return false;
+  const size_t mine = std::max(ls.held, need);
+  s->held_total += mine - ls.held;
+  ls.held = mine;
+  ls.busy = true;
+  return true;
+}
+
+void worker_loop(fsgc_server* s, int li) {
+  std::vector<uint64_t> batch;
+  std::vector<fsgc_task> tasks;
+  std::vector<fsgc_result> results;
+  std::vector<int> status;
+  for (;;) {
+    batch.clear();
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      LaneSlot& ls = s->lanes[(size_t)li];
+      for (;;) {
+        if (s->waiting.empty() && s->stop) return;
+        if (!s->waiting.empty()) {
+          if (admit(s, ls, batch)) break;
+          if (ls.held > 0) {
+            // the head does not fit: give back this idle lane's arena and let
+            // the other idle lanes do the same
+            fsgc_lane_trim(ls.lane);
+            s->held_total -= ls.held;
+            ls.held = 0;
+            s->cv_work.notify_all();
+            continue;
+          }
+        }
+        s->cv_work.wait(lk);
+      }
+      tasks.resize(batch.size());
+      for (size_t i = 0; i < batch.size(); i++) {
+        const Query& q = s->queries[batch[i]];
+        tasks[i].gid = q.gid;
+        tasks[i].mo = q.mo;
+      }
+    }
+    fsgc_lane* lane = s->lanes[(size_t)li].lane;
+    results.assign(batch.size(), fsgc_result{});
+    status.assign(batch.size(), FSGC_OK);
+    int st = fsgc_lane_submit(lane, tasks.data(), (int)tasks.size());
+    if (st == FSGC_OK) st = fsgc_lane_wait(lane, results.data());
+    if (st != FSGC_OK) {
+      if (batch.size() > 1) {
+        for (size_t i = 0; i < batch.size(); i++) {
+          status[i] = fsgc_lane_submit(lane, &tasks[i], 1);
+          if (status[i] == FSGC_OK) status[i] = fsgc_lane_wait(lane, &results[i]);
+        }
+      } else {
+        status[0] = st;
+      }
+    }
+    const auto now = Clock::now();
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      LaneSlot& ls = s->lanes[(size_t)li];
+      s->rounds++;
+      for (size_t i = 0; i < batch.size(); i++) {
+        Query& q = s->queries[batch[i]];
+        q.status = status[i];
+        q.result = results[i];
+        q.done = true;
+        q.latency_ms = std::chrono::duration<double, std::milli>(now - q.submitted).count();
+        s->latencies.push_back(q.latency_ms);
+        s->completed++;
+      }
+      // the arena now held, as allocated
+      const size_t real = fsgc_lane_scratch_bytes(lane);
+      s->held_total = s->held_total - ls.held + real;
+      ls.held = real;
+      ls.busy = false;
+      s->last_done = now;
+    }
+    s->cv_done.notify_all();
+    s->cv_work.notify_all();
+  }
+}
+
+double percentile(std::vector<double> v, double p) {
+  if (v.empty()) return 0;
+  std::sort(v.begin(), v.end());
+  const double idx = p * (double)(v.size() - 1);
+  const size_t lo = (size_t)idx;
+  const size_t hi = std::min(lo + 1, v.size() - 1);
+  return v[lo] + (v[hi] - v[lo]) * (idx - (double)lo);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fsgc_server_create(fsgc_ctx* ctx, size_t memory_budget, int lanes, int max_batch, fsgc_server** out) {
+  if (!ctx || !out || memory_budget == 0 || lanes < 1 || lanes > 64 || max_batch < 1) return FSGC_EINVAL;
+  *out = nullptr;
+  fsgc_server* s = new fsgc_server();
+  s->ctx = ctx;
+  s->budget = memory_budget;
+  s->max_batch = max_batch;
+  s->lanes.resize((size_t)lanes);
+  for (int i = 0; i < lanes; i++) {
+    const int st = fsgc_lane_create(ctx, &s->lanes[(size_t)i].lane);
+    if (st != FSGC_OK) {
+      for (int j = 0; j < i; j++) fsgc_lane_destroy(s->lanes[(size_t)j].lane);
+      delete s;
+      return st;
+    }
+  }
+  for (int i = 0; i < lanes; i++) s->workers.emplace_back(worker_loop, s, i);
+  *out = s;
+  return FSGC_OK;
+}
+
+void fsgc_server_destroy(fsgc_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  for (auto& w : s->workers)
+    if (w.joinable()) w.join();
+  for (auto& l : s->lanes) fsgc_lane_destroy(l.lane);
+  delete s;
+}
+
+int fsgc_server_add_graph(fsgc_server* s, int gid) {
+  if (!s) return FSGC_EINVAL;
+  const int st = fsgc_graph_prepare(s->ctx, gid);
+  if (st != FSGC_OK) return st;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->graphs[gid] = 1;
+  return FSGC_OK;
+}
+
+int fsgc_server_submit(fsgc_server* s, int gid, const fsgc_matching_order* mo, uint64_t* ticket) {
+  if (!s || !mo || !ticket) return FSGC_EINVAL;
+  const auto t0 = Clock::now();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->graphs.find(gid) == s->graphs.end()) return FSGC_ENOTFOUND;
+  }
+  fsgc_task task;
+  task.gid = gid;
+  task.mo = *mo;
+  size_t fp = 0;
+  const int st = fsgc_task_footprint(s->ctx, &task, &fp);
+  if (st != FSGC_OK) return st;
+  if (fp > s->budget) return FSGC_EBUSY;  // can never be admitted
+  std::lock_guard<std::mutex> lk(s->mu);
+  Query q;
+  q.ticket = s->next_ticket++;
+  q.gid = gid;
+  q.mo = *mo;
+  q.footprint = fp;
+  q.submitted = t0;
+  if (!s->any) {
+    s->first_submit = t0;
+    s->any = true;
+  }
+  s->queries[q.ticket] = q;
+  s->waiting.push_back(q.ticket);
+  *ticket = q.ticket;
+  s->cv_work.notify_one();
+  return FSGC_OK;
+}
+
+static int take_result(fsgc_server* s, uint64_t ticket, fsgc_result* out, double* latency_ms) {
+  auto it = s->queries.find(ticket);
+  Query& q = it->second;
+  const int st = q.status;
+  if (out) *out = q.result;
+  if (latency_ms) *latency_ms = q.latency_ms;
+  s->queries.erase(it);
+  return st;
+}
+
+int fsgc_server_poll(fsgc_server* s, uint64_t ticket, fsgc_result* out, double* latency_ms) {
+  if (!s) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->queries.find(ticket);
+  if (it == s->queries.end()) return FSGC_ENOTFOUND;
+  if (!it->second.done) return FSGC_EBUSY;
+  return take_result(s, ticket, out, latency_ms);
+}
+
+int fsgc_server_wait(fsgc_server* s, uint64_t ticket, double timeout_s, fsgc_result* out, double* latency_ms) {
+  if (!s) return FSGC_EINVAL;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto ready = [&] {
+    auto it = s->queries.find(ticket);
+    return it == s->queries.end() || it->second.done;
+  };
+  if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) return FSGC_ETIMEDOUT;
+  if (s->queries.find(ticket) == s->queries.end()) return FSGC_ENOTFOUND;
+  return take_result(s, ticket, out, latency_ms);
+}
+
+int fsgc_server_stats_get(fsgc_server* s, fsgc_server_stats* out) {
+  if (!s || !out) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  memset(out, 0, sizeof(*out));
+  out->completed = s->completed;
+  out->rounds = s->rounds;
+  out->queued = s->waiting.size();
+  out->in_use_bytes = s->held_total;
+  out->p50_ms = percentile(s->latencies, 0.50);
+  out->p99_ms = percentile(s->latencies, 0.99);
+  if (s->completed > 0 && s->any) {
+    const double secs = std::chrono::duration<double>(s->last_done - s->first_submit).count();
+    out->queries_per_s = secs > 0 ? (double)s->completed / secs : 0;
+  }
+  return FSGC_OK;
+}
+
+}  // extern "C"

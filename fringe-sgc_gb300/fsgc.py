@@ -54,6 +54,12 @@ class GraphInfo(C.Structure):
                 ("device_bytes", C.c_int64)]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_uint64), ("rounds", C.c_uint64), ("queued", C.c_uint64),
+                ("in_use_bytes", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("queries_per_s", C.c_double)]
+
+
 class FsgcError(RuntimeError):
     pass
 
@@ -105,6 +111,21 @@ def lib():
             "fsgc_ctx_set_exact_placements": (I, [P, I]),
             "fsgc_count_wedge_noalloc": (I, [I, I64, P, P, C.POINTER(MatchingOrder), P, C.POINTER(Result),
                                              C.c_char_p, I]),
+            "fsgc_lane_create": (I, [P, C.POINTER(P)]),
+            "fsgc_lane_destroy": (None, [P]),
+            "fsgc_lane_submit": (I, [P, C.POINTER(Task), I]),
+            "fsgc_lane_wait": (I, [P, C.POINTER(Result)]),
+            "fsgc_lane_query": (I, [P]),
+            "fsgc_lane_scratch_bytes": (C.c_size_t, [P]),
+            "fsgc_lane_trim": (I, [P]),
+            "fsgc_task_footprint": (I, [P, C.POINTER(Task), C.POINTER(C.c_size_t)]),
+            "fsgc_server_create": (I, [P, C.c_size_t, I, I, C.POINTER(P)]),
+            "fsgc_server_destroy": (None, [P]),
+            "fsgc_server_add_graph": (I, [P, I]),
+            "fsgc_server_submit": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(U64)]),
+            "fsgc_server_poll": (I, [P, U64, C.POINTER(Result), C.POINTER(C.c_double)]),
+            "fsgc_server_wait": (I, [P, U64, C.c_double, C.POINTER(Result), C.POINTER(C.c_double)]),
+            "fsgc_server_stats_get": (I, [P, C.POINTER(ServerStats)]),
             "fsgc_nck_host": (C.c_ulonglong, [I, I]),
             "fsgc_div_small_host": (C.c_ulonglong, [C.c_ulonglong, C.c_uint]),
         }
@@ -351,3 +372,107 @@ class Context:
         res = (Result * len(tasks))()
         _check(lib().fsgc_count_batch(self.ptr, arr, len(tasks), res), "count_batch", self.ptr)
         return list(res)
+
+
+# ----------------------------------------------------------------- lanes, serving
+class Lane:
+    """Asynchronous counts on their own stream: submit(tasks) returns at once,
+    wait() returns the results (as Context.count_batch would)."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        p = C.c_void_p()
+        _check(lib().fsgc_lane_create(ctx.ptr, C.byref(p)), "lane_create", ctx.ptr)
+        self.ptr = p
+        self.n = 0
+
+    def submit(self, tasks):
+        arr = (Task * len(tasks))()
+        for i, (gid, mo) in enumerate(tasks):
+            arr[i].gid = gid
+            arr[i].mo = mo
+        _check(lib().fsgc_lane_submit(self.ptr, arr, len(tasks)), "lane_submit", self.ctx.ptr)
+        self.n = len(tasks)
+
+    def done(self):
+        return lib().fsgc_lane_query(self.ptr) == 0
+
+    def wait(self):
+        res = (Result * self.n)()
+        _check(lib().fsgc_lane_wait(self.ptr, res), "lane_wait", self.ctx.ptr)
+        return list(res)
+
+    def scratch_bytes(self):
+        return lib().fsgc_lane_scratch_bytes(self.ptr)
+
+    def close(self):
+        if self.ptr:
+            lib().fsgc_lane_destroy(self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def task_footprint(ctx, gid, mo):
+    t = Task()
+    t.gid = gid
+    t.mo = mo
+    b = C.c_size_t()
+    _check(lib().fsgc_task_footprint(ctx.ptr, C.byref(t), C.byref(b)), "task_footprint", ctx.ptr)
+    return b.value
+
+
+class Server:
+    """Serving loop over a Context with continuous batching on `lanes` lanes:
+    submit() queues a count query and returns a ticket, wait() returns
+    (Result, latency_ms)."""
+
+    def __init__(self, ctx, memory_budget, lanes=4, max_batch=64):
+        self.ctx = ctx
+        p = C.c_void_p()
+        st = lib().fsgc_server_create(ctx.ptr, int(memory_budget), int(lanes), int(max_batch), C.byref(p))
+        _check(st, "server_create")
+        self.ptr = p
+
+    def add_graph(self, gid):
+        _check(lib().fsgc_server_add_graph(self.ptr, gid), "server_add_graph", self.ctx.ptr)
+
+    def submit(self, gid, mo):
+        t = C.c_uint64()
+        _check(lib().fsgc_server_submit(self.ptr, gid, C.byref(mo), C.byref(t)), "server_submit")
+        return t.value
+
+    def poll(self, ticket):
+        """None while the query runs, else (Result, latency_ms)."""
+        r, lat = Result(), C.c_double()
+        st = lib().fsgc_server_poll(self.ptr, ticket, C.byref(r), C.byref(lat))
+        if st == 8:  # FSGC_EBUSY
+            return None
+        _check(st, "server_poll", self.ctx.ptr)
+        return r, lat.value
+
+    def wait(self, ticket, timeout_s=600.0):
+        r, lat = Result(), C.c_double()
+        _check(lib().fsgc_server_wait(self.ptr, ticket, float(timeout_s), C.byref(r), C.byref(lat)), "server_wait",
+               self.ctx.ptr)
+        return r, lat.value
+
+    def stats(self):
+        s = ServerStats()
+        _check(lib().fsgc_server_stats_get(self.ptr, C.byref(s)), "server_stats")
+        return s
+
+    def close(self):
+        if self.ptr:
+            lib().fsgc_server_destroy(self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

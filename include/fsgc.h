@@ -181,6 +181,63 @@ typedef struct fsgc_task {
 } fsgc_task;
 int fsgc_count_batch(fsgc_ctx* ctx, const fsgc_task* tasks, int ntasks, fsgc_result* results);
 
+/* ---- lanes: asynchronous counts (no counterpart in the reference) ----
+ * A lane is a CUDA stream of the context with its own work areas and result
+ * slots.  fsgc_lane_submit checks a batch of tasks, builds any one-time
+ * per-graph structure they need (on the context's stream, synchronously) and
+ * enqueues the counts on the lane, then returns; fsgc_lane_wait sleeps until
+ * they finish and writes ntasks results (same values as fsgc_count_batch).
+ * Submissions on different lanes run concurrently on the device.  A lane holds
+ * one submission at a time (FSGC_EBUSY otherwise) and is used by one host
+ * thread at a time; destroy lanes before their context. */
+typedef struct fsgc_lane fsgc_lane;
+int fsgc_lane_create(fsgc_ctx* ctx, fsgc_lane** out);
+void fsgc_lane_destroy(fsgc_lane* lane);
+int fsgc_lane_submit(fsgc_lane* lane, const fsgc_task* tasks, int ntasks);
+int fsgc_lane_wait(fsgc_lane* lane, fsgc_result* results);
+/* FSGC_OK when the submission has finished, FSGC_EBUSY while it runs. */
+int fsgc_lane_query(fsgc_lane* lane);
+/* Device bytes of the lane's growable work arena, and its release (idle lane). */
+size_t fsgc_lane_scratch_bytes(const fsgc_lane* lane);
+int fsgc_lane_trim(fsgc_lane* lane);
+/* Work-arena bytes a count of this task needs beyond its resident graph
+ * (hub cursors of the wedge core, the triangle core's bitmaps); prepares the
+ * graph if it is not prepared yet. */
+int fsgc_task_footprint(fsgc_ctx* ctx, const fsgc_task* task, size_t* bytes);
+
+/* ---- serving loop (no counterpart in the reference, which runs one fringeCount
+ *      process per query: src/fringeCount.cu:2265-2331) ----
+ * Continuous batching over `lanes` lanes of `ctx`, one worker thread each.
+ * Graphs are uploaded to the context first and registered with
+ * fsgc_server_add_graph (which prepares them).  Submitted queries wait in
+ * arrival order.  Whenever a lane is free, its worker admits queries from the
+ * head of the queue (at most `max_batch`) while the lanes' work arenas, with
+ * this batch's need, fit `memory_budget`; it submits them to its lane and
+ * completes them when they finish, while the other lanes keep admitting and
+ * running queries that arrived in the meantime.  A query whose footprint alone
+ * exceeds the budget is refused at submission (FSGC_EBUSY); a query that fails
+ * fails alone.  Latency is submission to completion. */
+typedef struct fsgc_server fsgc_server;
+typedef struct fsgc_server_stats {
+  uint64_t completed;    /* queries finished */
+  uint64_t rounds;       /* lane submissions (batches) run */
+  uint64_t queued;       /* queries waiting for admission */
+  uint64_t in_use_bytes; /* work-arena bytes the lanes hold or have reserved */
+  double p50_ms, p99_ms; /* latency percentiles over completed queries */
+  double queries_per_s;  /* completed / (last completion - first submission) */
+} fsgc_server_stats;
+int fsgc_server_create(fsgc_ctx* ctx, size_t memory_budget, int lanes, int max_batch, fsgc_server** out);
+/* Finishes every submitted query, then stops the worker. */
+void fsgc_server_destroy(fsgc_server* srv);
+int fsgc_server_add_graph(fsgc_server* srv, int gid);
+int fsgc_server_submit(fsgc_server* srv, int gid, const fsgc_matching_order* mo, uint64_t* ticket);
+/* FSGC_EBUSY while the query runs; otherwise the query's own status, its result
+ * and latency, after which the ticket is forgotten. */
+int fsgc_server_poll(fsgc_server* srv, uint64_t ticket, fsgc_result* out, double* latency_ms);
+/* Blocks up to timeout_s seconds (FSGC_ETIMEDOUT), else as fsgc_server_poll. */
+int fsgc_server_wait(fsgc_server* srv, uint64_t ticket, double timeout_s, fsgc_result* out, double* latency_ms);
+int fsgc_server_stats_get(fsgc_server* srv, fsgc_server_stats* out);
+
 /* ---- allocation-free count (no counterpart in the reference) ----
  * For callers that cannot allocate device memory when they count -- code
  * running where a host framework forbids cudaMalloc after start-up, or inside
