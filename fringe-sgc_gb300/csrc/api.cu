@@ -93,6 +93,7 @@ void free_graph(DevGraph* g) {
   cudaFree(g->osrc);
   cudaFree(g->osup);
   cudaFree(g->vtri2);
+  cudaFree(g->esup);
   cudaFree(g->ctab_id);
   cudaFree(g->ctab_rows);
   cudaFree(g->ctab_pos);

@@ -786,7 +786,8 @@ struct GWedgeParams {
 // warp per centre u, looping over endpoints v in N(u); lanes take w in N(u),
 // w < v; open wedges use rotations 0 (and 3), triangles (counted once, with
 // u < w < v) use all rotations.
-__global__ void wedge_general_kernel(GView g, GWedgeParams p, u64* __restrict__ slot) {
+__global__ void wedge_general_kernel(GView g, GWedgeParams p, const unsigned* __restrict__ esup,
+                                     u64* __restrict__ slot) {
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -811,15 +812,7 @@ __global__ void wedge_general_kernel(GView g, GWedgeParams p, u64* __restrict__ 
       const int dv = g.deg[v];
       if (dv < th1u) continue;  // init_wl_wedge
       const int* Nv = g.adj + g.off[v];
-      // p12 = |N(u) & N(v)|
-      int p12 = 0;
-      {
-        const int* S = (du <= dv) ? Nu : Nv;
-        const int* L = (du <= dv) ? Nv : Nu;
-        const int ls = min(du, dv), ll = max(du, dv);
-        for (int t = lane; t < ls; t += 32) p12 += bsearch_has(L, ll, __ldg(S + t));
-        p12 = __reduce_add_sync(0xffffffffu, p12);
-      }
+      const int p12 = (int)__ldg(esup + j);  // |N(u) & N(v)|
       const bool cond = (du >= p.min_u) && (dv >= p.lim);
       const int thres1 = max(p.lim, p.sum2 - dv);
       const int thres2 = max(max(p.sum1, p.sum3 - du - dv), max(p.sum2 - du, p.sum2 - dv));
@@ -839,23 +832,30 @@ __global__ void wedge_general_kernel(GView g, GWedgeParams p, u64* __restrict__ 
         }
         if (!__any_sync(0xffffffffu, t < du && w < v)) break;
         unsigned bal = __ballot_sync(0xffffffffu, active);
-        int t13 = 0, t23 = 0, t123 = 0;
+        // |N(u) & N(w)| is the support of the entry (u, w); |N(v) & N(w)|
+        // and the triple overlap walk the shorter of N(v), N(w)
+        const int t13 = active ? (int)__ldg(esup + ub + t) : 0;
+        int t23 = 0, t123 = 0;
         while (bal) {
           const int who = __ffs(bal) - 1;
           bal &= bal - 1;
           const int ww = __shfl_sync(0xffffffffu, w, who);
           const int dww = __shfl_sync(0xffffffffu, dw, who);
           const int* Nw = g.adj + g.off[ww];
-          int a13 = 0, a23 = 0, a123 = 0;
-          for (int q = lane; q < dww; q += 32) {
-            const int x = __ldg(Nw + q);
-            const bool b13 = bsearch_has(Nu, du, x), b23 = bsearch_has(Nv, dv, x);
-            a13 += b13; a23 += b23; a123 += (b13 && b23);
+          const int* S = (dww <= dv) ? Nw : Nv;
+          const int* L = (dww <= dv) ? Nv : Nw;
+          const int ls = min(dww, dv), ll = max(dww, dv);
+          int a23 = 0, a123 = 0;
+          for (int q = lane; q < ls; q += 32) {
+            const int x = __ldg(S + q);
+            if (bsearch_has(L, ll, x)) {
+              a23++;
+              a123 += bsearch_has(Nu, du, x);
+            }
           }
-          a13 = __reduce_add_sync(0xffffffffu, a13);
           a23 = __reduce_add_sync(0xffffffffu, a23);
           a123 = __reduce_add_sync(0xffffffffu, a123);
-          if (lane == who) { t13 = a13; t23 = a23; t123 = a123; }
+          if (lane == who) { t23 = a23; t123 = a123; }
         }
         if (active) {
           // common3_wedge (src/fringeCount.cu:1480-1510) + corrections
@@ -1250,6 +1250,7 @@ namespace {
 struct Needs {
   bool chunk_table = false;  // wedge core with a fringe-free centre
   bool vertex_triangles = false;
+  bool entry_supports = false;  // general wedge core
   size_t scratch = 0;        // arena bytes (hub cursors, triangle bitmaps)
 };
 
@@ -1277,6 +1278,8 @@ Needs needs_of(const fsgc_matching_order& mo, const DevGraph& G) {
         const long long gs = G.maxdeg;
         nd.scratch = (size_t)sm_count() * ((size_t)2 * gs * sizeof(long long) + (size_t)(gs + 1) * sizeof(int));
       }
+    } else {
+      nd.entry_supports = true;
     }
     return nd;
   }
@@ -1306,6 +1309,10 @@ int prepare_for_count(const fsgc_matching_order& mo, DevGraph& G, cudaStream_t s
   }
   if (nd.vertex_triangles) {
     st = ensure_vertex_triangles(G, s, launches);
+    if (st != FSGC_OK) return st;
+  }
+  if (nd.entry_supports) {
+    st = ensure_entry_supports(G, s, launches);
     if (st != FSGC_OK) return st;
   }
   return cudaStreamSynchronize(s) == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
@@ -1426,7 +1433,9 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
     GWedgeParams gp;
     gp.min_u = min_u; gp.lim = lim; gp.sum1 = sum1; gp.sum2 = sum2; gp.sum3 = sum3;
     rotations3(f, true, gp.rot);
-    wedge_general_kernel<<<grid_for(G.m * 32, TPB, 8), TPB, 0, s>>>(gv, gp, job.d_slot);
+    st = ensure_entry_supports(G, s, launches);
+    if (st != FSGC_OK) return st;
+    wedge_general_kernel<<<grid_for(G.m * 32, TPB, 8), TPB, 0, s>>>(gv, gp, G.esup, job.d_slot);
     *launches += 1;
     return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
   }

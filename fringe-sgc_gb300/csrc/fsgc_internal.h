@@ -51,6 +51,7 @@ struct DevGraph {
   long long max_outdeg = 0;        // largest oriented out-degree
   long long max_bitmap_words = 0;  // max over v of outdeg(v) * ceil(deg(v) / 32)
   u64* vtri2 = nullptr;  // lazily
+  unsigned* esup = nullptr;  // lazily: per list entry (u, v), |N(u) & N(v)|
   // wedge core: offsets of chunk boundaries in the lists of high-degree vertices (lazily)
   int* ctab_id = nullptr;
   int* ctab_rows = nullptr;
@@ -98,6 +99,7 @@ struct Launcher;  // forward
 int graph_degrees(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_scratch_u64);
 int prepare_graph(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_scratch_u64);
 int ensure_vertex_triangles(DevGraph& g, cudaStream_t s, uint64_t* launches);
+int ensure_entry_supports(DevGraph& g, cudaStream_t s, uint64_t* launches);
 void upload_div_magic();
 int sm_count();
 

@@ -231,6 +231,20 @@ __global__ void vertex_triangle_kernel(GView g, u64* __restrict__ vtri2) {
   }
 }
 
+// The support of each oriented edge, written to both of its list entries.
+__global__ void entry_support_kernel(GView g, unsigned* __restrict__ esup) {
+  const long long me = g.m / 2;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < me; j += (long long)gridDim.x * blockDim.x) {
+    const int a = g.osrc[j], b = g.oadj[j];
+    const unsigned s = g.osup[j];
+    const long long oa = g.off[a], ob = g.off[b];
+    const int pa = bsearch_pos(g.adj + oa, (int)(g.off[a + 1] - oa), b);
+    const int pb = bsearch_pos(g.adj + ob, (int)(g.off[b + 1] - ob), a);
+    if (pa >= 0) esup[oa + pa] = s;
+    if (pb >= 0) esup[ob + pb] = s;  // absent only in a non-symmetric input
+  }
+}
+
 int g_sms = 0;
 
 }  // namespace
@@ -327,6 +341,20 @@ int prepare_graph(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_u64) {
   g.tri_relabel = (n > 10000) && !((long long)n > g.m / 10) && (maxd > 16);
   g.bytes += sizeof(long long) * ((size_t)n + 1) + (sizeof(int) * 2 + sizeof(unsigned)) * (size_t)std::max(1LL, me);
   g.prepared = true;
+  return FSGC_OK;
+}
+
+int ensure_entry_supports(DevGraph& g, cudaStream_t s, uint64_t* launches) {
+  if (g.esup) return FSGC_OK;
+  FSGC_TRY(cudaMallocAsync((void**)&g.esup, sizeof(unsigned) * (size_t)std::max(1LL, g.m), s));
+  FSGC_TRY(cudaMemsetAsync(g.esup, 0, sizeof(unsigned) * (size_t)std::max(1LL, g.m), s));
+  const long long me = g.m / 2;
+  if (me > 0) {
+    entry_support_kernel<<<grid_for(me, kTPB, 8), kTPB, 0, s>>>(g.view(), g.esup);
+    *launches += 1;
+  }
+  g.bytes += sizeof(unsigned) * (size_t)std::max(1LL, g.m);
+  FSGC_TRY(cudaGetLastError());
   return FSGC_OK;
 }
 
