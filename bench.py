@@ -468,9 +468,9 @@ def main():
                          "serve: the serving loop")
     ap.add_argument("--graphs", type=int, default=256, help="packed: member graphs")
     ap.add_argument("--nmax", type=int, default=50000, help="packed: largest member size")
-    ap.add_argument("--serve-scales", default="10,11,12,13,14,15,16,17", help="serve: RMAT scales")
-    ap.add_argument("--queries", type=int, default=2000, help="serve: queries")
-    ap.add_argument("--rate", type=float, default=500.0, help="serve: Poisson arrivals per second")
+    ap.add_argument("--serve-scales", default="6,7,8,9,10,11,12,13", help="serve: RMAT scales")
+    ap.add_argument("--queries", type=int, default=300, help="serve: queries")
+    ap.add_argument("--rate", type=float, default=5.0, help="serve: Poisson arrivals per second")
     ap.add_argument("--lanes", type=int, default=4, help="serve: lanes")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serve: work-arena budget")
     ap.add_argument("--gpus", type=int, default=1)
