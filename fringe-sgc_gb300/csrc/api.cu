@@ -55,7 +55,8 @@ struct fsgc_lane {
   std::vector<fsgc::CountJob> jobs;
   std::vector<u64> aut;
   std::vector<fsgc_result> res;
-  int pending = 0;
+  int pending = 0;   // tasks of the submission in flight (0: the lane is free)
+  int finished = 0;  // tasks whose results have been taken
 };
 
 namespace {
@@ -272,9 +273,11 @@ int plan_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, std::vector<u64>& au
 }
 
 // Enqueues a planned batch on `s`: slot reset, each task's kernels between
-// events ev[t] and ev[t+1], and the read-back of the raw totals into h_slots.
+// events ev[t] and ev[t+1], and the read-back of the raw totals into h_slots
+// (per task before its closing event when per_task_copy, else once at the end).
 int enqueue_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, cudaStream_t s, fsgc::DevWork& work, u64* d_slots,
-                  u64* h_slots, const cudaEvent_t* ev, std::vector<fsgc::CountJob>& jobs, fsgc_result* res) {
+                  u64* h_slots, const cudaEvent_t* ev, std::vector<fsgc::CountJob>& jobs, fsgc_result* res,
+                  bool per_task_copy) {
   jobs.assign((size_t)nt, fsgc::CountJob{});
   CK(cudaMemsetAsync(d_slots, 0, sizeof(u64) * (size_t)nt, s), "slot reset");
   CK(cudaEventRecord(ev[0], s), "event");
@@ -296,27 +299,28 @@ int enqueue_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, cudaStream_t s, f
         return fail(c, st, "task %d: count failed (%s)", t, cudaGetErrorString(cudaGetLastError()));
       }
     }
+    if (per_task_copy)
+      CK(cudaMemcpyAsync(h_slots + t, d_slots + t, sizeof(u64), cudaMemcpyDeviceToHost, s), "readback");
     CK(cudaEventRecord(ev[t + 1], s), "event");
   }
-  CK(cudaMemcpyAsync(h_slots, d_slots, sizeof(u64) * (size_t)nt, cudaMemcpyDeviceToHost, s), "readback");
+  if (!per_task_copy)
+    CK(cudaMemcpyAsync(h_slots, d_slots, sizeof(u64) * (size_t)nt, cudaMemcpyDeviceToHost, s), "readback");
   return FSGC_OK;
 }
 
-// Results of a finished batch (its stream has completed).
-void finish_tasks(int nt, const std::vector<fsgc::CountJob>& jobs, const std::vector<u64>& aut, const u64* h_slots,
-                  const cudaEvent_t* ev, fsgc_result* res) {
-  for (int t = 0; t < nt; t++) {
-    const u64 raw = jobs[t].host_only ? jobs[t].host_value : h_slots[t];
-    const bool too_large = (res[t].flags & FSGC_FLAG_PATTERN_TOO_LARGE) != 0;
-    res[t].raw_total = raw;
-    // no divisor is computed when the pattern does not fit the graph
-    res[t].automorphisms = too_large ? 0 : aut[t];
-    res[t].count = too_large ? 0 : raw / aut[t];
-    res[t].core_type = jobs[t].core_type;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ev[t], ev[t + 1]);
-    res[t].device_ms = ms;
-  }
+// Result of finished task t (its closing event and read-back have completed).
+void finish_task(int t, const std::vector<fsgc::CountJob>& jobs, const std::vector<u64>& aut, const u64* h_slots,
+                 const cudaEvent_t* ev, fsgc_result* res) {
+  const u64 raw = jobs[t].host_only ? jobs[t].host_value : h_slots[t];
+  const bool too_large = (res[t].flags & FSGC_FLAG_PATTERN_TOO_LARGE) != 0;
+  res[t].raw_total = raw;
+  // no divisor is computed when the pattern does not fit the graph
+  res[t].automorphisms = too_large ? 0 : aut[t];
+  res[t].count = too_large ? 0 : raw / aut[t];
+  res[t].core_type = jobs[t].core_type;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev[t], ev[t + 1]);
+  res[t].device_ms = ms;
 }
 
 int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
@@ -330,10 +334,10 @@ int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
   st = plan_tasks(c, tasks, nt, aut);
   if (st != FSGC_OK) return st;
   std::vector<fsgc::CountJob> jobs;
-  st = enqueue_tasks(c, tasks, nt, c->stream, c->work, c->d_slots, c->h_slots, c->events.data(), jobs, res);
+  st = enqueue_tasks(c, tasks, nt, c->stream, c->work, c->d_slots, c->h_slots, c->events.data(), jobs, res, false);
   if (st != FSGC_OK) return st;
   CK(cudaStreamSynchronize(c->stream), "count");
-  finish_tasks(nt, jobs, aut, c->h_slots, c->events.data(), res);
+  for (int t = 0; t < nt; t++) finish_task(t, jobs, aut, c->h_slots, c->events.data(), res);
   return FSGC_OK;
 }
 
@@ -753,26 +757,37 @@ int fsgc_lane_submit(fsgc_lane* L, const fsgc_task* tasks, int ntasks) {
   }
   L->res.assign((size_t)ntasks, fsgc_result{});
   st = enqueue_tasks(c, L->tasks.data(), ntasks, L->stream, L->work, L->d_slots, L->h_slots, L->events.data(),
-                     L->jobs, L->res.data());
+                     L->jobs, L->res.data(), true);
   if (st != FSGC_OK) return st;
-  CK(cudaEventRecord(L->events[(size_t)ntasks], L->stream), "event");
   L->pending = ntasks;
+  L->finished = 0;
+  return FSGC_OK;
+}
+
+int fsgc_lane_wait_task(fsgc_lane* L, int index, fsgc_result* out) {
+  if (!L) return FSGC_EINVAL;
+  if (L->pending <= 0 || index < L->finished || index >= L->pending) return FSGC_ENOTFOUND;
+  cudaSetDevice(L->ctx->device);
+  // the host thread sleeps until the task's closing event (blocking-sync event)
+  const cudaError_t e = cudaEventSynchronize(L->events[(size_t)index + 1]);
+  if (e != cudaSuccess) {
+    L->pending = 0;
+    std::lock_guard<std::mutex> lk(L->ctx->mu);
+    return cuda_fail(L->ctx, e, "lane count");
+  }
+  for (int t = L->finished; t <= index; t++) finish_task(t, L->jobs, L->aut, L->h_slots, L->events.data(), L->res.data());
+  L->finished = index + 1;
+  if (out) *out = L->res[(size_t)index];
+  if (L->finished == L->pending) L->pending = 0;  // the lane is free again
   return FSGC_OK;
 }
 
 int fsgc_lane_wait(fsgc_lane* L, fsgc_result* results) {
   if (!L) return FSGC_EINVAL;
   if (L->pending <= 0) return FSGC_ENOTFOUND;
-  cudaSetDevice(L->ctx->device);
-  // the host thread sleeps until the lane's last event (blocking-sync event)
-  const cudaError_t e = cudaEventSynchronize(L->events[(size_t)L->pending]);
   const int nt = L->pending;
-  L->pending = 0;
-  if (e != cudaSuccess) {
-    std::lock_guard<std::mutex> lk(L->ctx->mu);
-    return cuda_fail(L->ctx, e, "lane count");
-  }
-  finish_tasks(nt, L->jobs, L->aut, L->h_slots, L->events.data(), L->res.data());
+  const int st = fsgc_lane_wait_task(L, nt - 1, nullptr);
+  if (st != FSGC_OK) return st;
   if (results) memcpy(results, L->res.data(), sizeof(fsgc_result) * (size_t)nt);
   return FSGC_OK;
 }
@@ -780,7 +795,7 @@ int fsgc_lane_wait(fsgc_lane* L, fsgc_result* results) {
 int fsgc_lane_query(fsgc_lane* L) {
   if (!L) return FSGC_EINVAL;
   if (L->pending <= 0) return FSGC_ENOTFOUND;
-  const cudaError_t e = cudaEventQuery(L->events[(size_t)L->pending]);
+  const cudaError_t e = cudaEventQuery(L->events[(size_t)L->pending]);  // the last task's closing event
   if (e == cudaErrorNotReady) return FSGC_EBUSY;
   return e == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }

@@ -489,12 +489,19 @@ constexpr int kWDvMax = 2048;
 constexpr int kWThreads = 1024;
 constexpr int kWGran = 32768;  // ids between the chunk boundaries in the boundary table
 
+// SMALL packs counters of 16, 8 or 4 bits into 32-bit words, the narrowest
+// that holds the owner's degree (a count C(v, w) never exceeds deg v), so one
+// chunk covers 65,536, 131,072 or 262,144 ids; BIG uses 32-bit counters.
 template <bool BIG>
 struct WedgeCfg {
-  static constexpr int CH = BIG ? 32768 : 65536;   // ids per chunk (multiple of kWGran)
+  static constexpr int CH = BIG ? 32768 : 65536;   // ids per chunk at 16-bit (BIG: 32-bit) counters
   static constexpr int WORDS = BIG ? CH : CH / 2;  // counter words
   static constexpr int TW = WORDS / 32;            // touched-bitmap words (= kWThreads)
+  static constexpr int CH_MAX = BIG ? CH : 4 * CH; // widest chunk (4-bit counters)
 };
+
+// counter width for an owner of degree dv (SMALL kernel)
+__device__ __forceinline__ int wedge_counter_bits(int dv) { return dv <= 15 ? 4 : (dv <= 255 ? 8 : 16); }
 static_assert(WedgeCfg<false>::TW == kWThreads && WedgeCfg<true>::TW == kWThreads, "one bitmap word per thread");
 
 template <bool BIG>
@@ -502,7 +509,7 @@ struct WedgeSmem {
   unsigned cnt[WedgeCfg<BIG>::WORDS];
   unsigned touched[WedgeCfg<BIG>::TW];  // counter words that became non-zero
   int tpre[WedgeCfg<BIG>::TW + 1];      // prefix of touched popcounts
-  unsigned adjbits[WedgeCfg<BIG>::CH / 32];
+  unsigned adjbits[WedgeCfg<BIG>::CH_MAX / 32];
   long long cur[BIG ? 1 : kWDvMax];
   long long lim[BIG ? 1 : kWDvMax];
   int pre[BIG ? 1 : kWDvMax + 1];
@@ -587,7 +594,6 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
                                                                    long long* __restrict__ gcur, int* __restrict__ gpre,
                                                                    long long gstride, ChunkTable tab,
                                                                    u64* __restrict__ slot) {
-  constexpr int CH = WedgeCfg<BIG>::CH;
   constexpr int WORDS = WedgeCfg<BIG>::WORDS;
   constexpr int TW = WedgeCfg<BIG>::TW;
   extern __shared__ unsigned char s_raw[];
@@ -598,7 +604,7 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
   int* pre = BIG ? gpre + (size_t)blockIdx.x * (gstride + 1) : S.pre;
   for (int i = tid; i < WORDS; i += blockDim.x) S.cnt[i] = 0;
   for (int i = tid; i < TW; i += blockDim.x) S.touched[i] = 0;
-  for (int i = tid; i < CH / 32; i += blockDim.x) S.adjbits[i] = 0;
+  for (int i = tid; i < WedgeCfg<BIG>::CH_MAX / 32; i += blockDim.x) S.adjbits[i] = 0;
   u64 acc = 0;
   for (;;) {
     if (tid == 0) {
@@ -614,6 +620,10 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
       continue;
     }
     const int thres = max(p.lim, p.minsum - dv);
+    // counter layout: `bits` per counter, 2^lper counters per word, CH ids per chunk
+    const int bits = BIG ? 32 : wedge_counter_bits(dv);
+    const int lper = BIG ? 0 : (bits == 16 ? 1 : (bits == 8 ? 2 : 3));
+    const int CH = WORDS << lper;
     const long long vb = g.off[v];
     const int* Nv = g.adj + vb;
     for (int t = tid; t < dv; t += blockDim.x) {
@@ -666,8 +676,8 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
             if (e < we) {
               while (pre[al + 1] <= e) al++;
               const int o = __ldg(g.adj + cur[al] + (e - pre[al])) - lo;
-              const int wd = BIG ? o : (o >> 1);
-              const unsigned old = atomicAdd(&S.cnt[wd], BIG ? 1u : (1u << ((o & 1) << 4)));
+              const int wd = o >> lper;
+              const unsigned old = atomicAdd(&S.cnt[wd], BIG ? 1u : (1u << ((o & ((1 << lper) - 1)) * bits)));
               if (old == 0) atomicOr(&S.touched[wd >> 5], 1u << (wd & 31));
             }
             a = __shfl_sync(0xffffffffu, al, 31);
@@ -678,7 +688,7 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
       // evaluate: prefix-sum the touched-word popcounts (one bitmap word per
       // thread) and give every thread an equal share of the touched words
       {
-        const int nw = BIG ? (hi - lo) : ((hi - lo + 1) >> 1);
+        const int nw = (hi - lo + (1 << lper) - 1) >> lper;
         const int ntw = (nw + 31) >> 5;
         const int c0 = (tid < ntw) ? __popc(S.touched[tid]) : 0;
         int inc = c0;
@@ -722,12 +732,14 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
               const int w = lo + wd;
               eval_pair<BIG>(g, p, S, lo, wd, word, g.deg[w], v, dv, thres, acc);
             } else {
-              const int o0 = 2 * wd;
-              const unsigned C0 = word & 0xffffu, C1 = word >> 16;
-              const int d0 = C0 ? g.deg[lo + o0] : 0;
-              const int d1 = C1 ? g.deg[lo + o0 + 1] : 0;
-              if (C0) eval_pair<BIG>(g, p, S, lo, o0, C0, d0, v, dv, thres, acc);
-              if (C1) eval_pair<BIG>(g, p, S, lo, o0 + 1, C1, d1, v, dv, thres, acc);
+              const int o0 = wd << lper;
+              const unsigned cmask = (bits == 16) ? 0xffffu : ((1u << bits) - 1);
+              for (unsigned rest = word; rest; ) {
+                const int k = (__ffs(rest) - 1) / bits;  // next non-zero counter of the word
+                const unsigned C = (word >> (k * bits)) & cmask;
+                rest &= ~(cmask << (k * bits));
+                eval_pair<BIG>(g, p, S, lo, o0 + k, C, g.deg[lo + o0 + k], v, dv, thres, acc);
+              }
             }
           }
         }
@@ -740,11 +752,11 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
         if (c < lim[t]) nxt = min(nxt, __ldg(g.adj + c));
       }
       nxt = __reduce_min_sync(0xffffffffu, nxt);
-      cv = cend;
       if (tid == 0) S.lo = v;
       __syncthreads();  // touched, adjbits, pre and S.lo are free again
       for (int i = tid; i < TW; i += blockDim.x) S.touched[i] = 0;
-      for (int i = tid; i < (CH >> 5); i += blockDim.x) S.adjbits[i] = 0;
+      for (int i = cs + tid; i < cend; i += blockDim.x) S.adjbits[(__ldg(Nv + i) - lo) >> 5] = 0;
+      cv = cend;
       if (lane == 0 && nxt < v) atomicMin(&S.lo, max(hi, (nxt / CH) * CH));
       __syncthreads();
     }

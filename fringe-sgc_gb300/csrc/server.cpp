@@ -8,9 +8,10 @@
 // queries from the head of the queue -- its share of what is waiting, at most
 // max_batch -- while the lanes' work arenas, grown to this batch's need, stay
 // within the memory budget, submits them to its lane and sleeps until they
-// finish.  Meanwhile the other workers admit and submit what arrives, so work
-// from different batches overlaps on the device and no query waits for a
-// batch that was already running when it arrived.  A batch that fails is
+// finish, completing each query as soon as its own counts are done.
+// Meanwhile the other workers admit and submit what arrives, so work from
+// different batches overlaps on the device and no query waits for a batch
+// that was already running when it arrived.  A batch the checks refuse is
 // re-run one query at a time, so that a bad query fails alone.  Latency is
 // submission to completion.
 #include <algorithm>
@@ -133,24 +134,11 @@ void worker_loop(fsgc_server* s, int li) {
     fsgc_lane* lane = s->lanes[(size_t)li].lane;
     results.assign(batch.size(), fsgc_result{});
     status.assign(batch.size(), FSGC_OK);
-    int st = fsgc_lane_submit(lane, tasks.data(), (int)tasks.size());
-    if (st == FSGC_OK) st = fsgc_lane_wait(lane, results.data());
-    if (st != FSGC_OK) {
-      if (batch.size() > 1) {
-        for (size_t i = 0; i < batch.size(); i++) {
-          status[i] = fsgc_lane_submit(lane, &tasks[i], 1);
-          if (status[i] == FSGC_OK) status[i] = fsgc_lane_wait(lane, &results[i]);
-        }
-      } else {
-        status[0] = st;
-      }
-    }
-    const auto now = Clock::now();
-    {
-      std::lock_guard<std::mutex> lk(s->mu);
-      LaneSlot& ls = s->lanes[(size_t)li];
-      s->rounds++;
-      for (size_t i = 0; i < batch.size(); i++) {
+    // each query completes as soon as its own counts have finished
+    auto complete = [&](size_t i) {
+      const auto now = Clock::now();
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
         Query& q = s->queries[batch[i]];
         q.status = status[i];
         q.result = results[i];
@@ -158,15 +146,38 @@ void worker_loop(fsgc_server* s, int li) {
         q.latency_ms = std::chrono::duration<double, std::milli>(now - q.submitted).count();
         s->latencies.push_back(q.latency_ms);
         s->completed++;
+        s->last_done = now;
       }
+      s->cv_done.notify_all();
+    };
+    int st = fsgc_lane_submit(lane, tasks.data(), (int)tasks.size());
+    if (st == FSGC_OK) {
+      for (size_t i = 0; i < batch.size(); i++) {
+        status[i] = (st == FSGC_OK) ? fsgc_lane_wait_task(lane, (int)i, &results[i]) : st;
+        st = status[i];
+        complete(i);
+      }
+    } else if (batch.size() > 1) {
+      // a batch the checks refused: each query on its own, so a bad one fails alone
+      for (size_t i = 0; i < batch.size(); i++) {
+        status[i] = fsgc_lane_submit(lane, &tasks[i], 1);
+        if (status[i] == FSGC_OK) status[i] = fsgc_lane_wait(lane, &results[i]);
+        complete(i);
+      }
+    } else {
+      status[0] = st;
+      complete(0);
+    }
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      LaneSlot& ls = s->lanes[(size_t)li];
+      s->rounds++;
       // the arena now held, as allocated
       const size_t real = fsgc_lane_scratch_bytes(lane);
       s->held_total = s->held_total - ls.held + real;
       ls.held = real;
       ls.busy = false;
-      s->last_done = now;
     }
-    s->cv_done.notify_all();
     s->cv_work.notify_all();
   }
 }

@@ -115,6 +115,7 @@ def lib():
             "fsgc_lane_destroy": (None, [P]),
             "fsgc_lane_submit": (I, [P, C.POINTER(Task), I]),
             "fsgc_lane_wait": (I, [P, C.POINTER(Result)]),
+            "fsgc_lane_wait_task": (I, [P, I, C.POINTER(Result)]),
             "fsgc_lane_query": (I, [P]),
             "fsgc_lane_scratch_bytes": (C.c_size_t, [P]),
             "fsgc_lane_trim": (I, [P]),
@@ -396,6 +397,11 @@ class Lane:
 
     def done(self):
         return lib().fsgc_lane_query(self.ptr) == 0
+
+    def wait_task(self, index):
+        r = Result()
+        _check(lib().fsgc_lane_wait_task(self.ptr, int(index), C.byref(r)), "lane_wait_task", self.ctx.ptr)
+        return r
 
     def wait(self):
         res = (Result * self.n)()

@@ -195,6 +195,10 @@ int fsgc_lane_create(fsgc_ctx* ctx, fsgc_lane** out);
 void fsgc_lane_destroy(fsgc_lane* lane);
 int fsgc_lane_submit(fsgc_lane* lane, const fsgc_task* tasks, int ntasks);
 int fsgc_lane_wait(fsgc_lane* lane, fsgc_result* results);
+/* Sleeps until task `index` of the submission has finished (tasks finish in
+ * order) and writes its result; take results in increasing index order.  The
+ * lane is free again once the last task's result has been taken. */
+int fsgc_lane_wait_task(fsgc_lane* lane, int index, fsgc_result* out);
 /* FSGC_OK when the submission has finished, FSGC_EBUSY while it runs. */
 int fsgc_lane_query(fsgc_lane* lane);
 /* Device bytes of the lane's growable work arena, and its release (idle lane). */

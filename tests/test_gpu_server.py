@@ -122,7 +122,10 @@ def test_lanes_overlap_and_match_batch(ctx):
         parts = [tasks[i::3] for i in range(3)]
         for lane, part in zip(lanes, parts):
             lane.submit(part)
-        got = [lane.wait() for lane in lanes]
+        # lane 1 hands its results out one task at a time, the others all at once
+        got = [lanes[0].wait(), [lanes[1].wait_task(i) for i in range(len(parts[1]))], lanes[2].wait()]
+        lanes[1].submit(parts[1][:1])  # free again once its last result was taken
+        assert lanes[1].wait()[0].count == want[1].count
         for i, part in enumerate(parts):
             assert len(got[i]) == len(part)
             for j, r in enumerate(got[i]):
