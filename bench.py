@@ -195,6 +195,20 @@ def kernel_bytes(name, core, g):
     return None
 
 
+def measured_traffic(pattern, g):
+    """DRAM bytes (read + write) of one count of `pattern` on this graph, from the
+    ncu capture recorded in profiles/dram_traffic.json (null when the capture
+    was of another pattern or graph size)."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        rec = json.load(f)
+    if rec.get("pattern") != pattern or rec.get("n") != g.n or rec.get("m") != g.m:
+        return None
+    return rec.get("dram_bytes")
+
+
 def max_over_ranks(values, world):
     """Replicas: the job's time is the slowest rank's (element-wise max over ranks)."""
     if world <= 1:
@@ -541,8 +555,8 @@ def main():
     if alg is not None and ms > 0:
         ach = alg / (ms / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(ach / peak, 4), "traffic": None, "kernel": dom, "kernel_ms": round(ms, 3),
-                "algorithmic_bytes": alg, "peak_kind": peak_kind}
+                "frac": round(ach / peak, 4), "traffic": measured_traffic(dom, g), "kernel": dom,
+                "kernel_ms": round(ms, 3), "algorithmic_bytes": alg, "peak_kind": peak_kind}
     cpu = None
     if world == 1 and args.cpu_budget > 0:
         est, samples = cpu_sample(g, mos, args.cpu_budget, os.cpu_count() or 1)

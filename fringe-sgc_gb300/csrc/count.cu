@@ -357,7 +357,7 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
 // iff bit pos(b_j) of M_i is set, |N(a) & N(b_i)| = popc(M_i), and the triple
 // overlap |N(a) & N(b_i) & N(b_j)| = popc(M_i & M_j) -- a few word operations
 // per triangle instead of an intersection of full neighbour lists.
-__global__ void __launch_bounds__(256) triangle_bitmap_kernel(GView g, TriParams p, int* __restrict__ queue,
+__global__ void __launch_bounds__(256, 3) triangle_bitmap_kernel(GView g, TriParams p, int* __restrict__ queue,
                                                               unsigned* __restrict__ bits_all, long long bits_per_block,
                                                               u64* __restrict__ slot) {
   extern __shared__ int s_dyn[];
@@ -1241,12 +1241,13 @@ int ensure_plain_scratch(Scratch& sc, size_t need, cudaStream_t s) {
 }
 
 // Triangle bitmap kernel geometry: rows of ceil(deg/32) words per out-neighbour
-// of the block's vertex, one arena of max_bitmap_words per block, at most 8 GiB.
+// of the block's vertex, one arena of max_bitmap_words per block, at most 8 GiB;
+// three resident blocks per SM (the kernel is built for 80 registers a thread).
 void triangle_bitmap_geometry(const DevGraph& G, long long* per_block, int* blocks) {
   *per_block = std::max(1LL, G.max_bitmap_words);
   const size_t budget = (size_t)8 << 30;
   *blocks = (int)std::max<size_t>(
-      1, std::min<size_t>((size_t)sm_count() * 4, budget / (sizeof(unsigned) * (size_t)*per_block)));
+      1, std::min<size_t>((size_t)sm_count() * 3, budget / (sizeof(unsigned) * (size_t)*per_block)));
 }
 
 bool triangle_uses_bitmaps(const fsgc_matching_order& mo, const DevGraph& G, int mode) {
