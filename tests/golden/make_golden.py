@@ -5,7 +5,7 @@ oracle/Makefile into oracle/_ref/) on
   - every pattern file of the reference's pattern corpus (patterns/**.txt),
     turned into a command line the way its harness does (reproduce.py:54-66);
   - the 31 predefined motifs (`fringePreprocess <number>`);
-  - the BASELINE workload patterns;
+  - the workload patterns (ER triangle + 2 fringes, the eight RMAT patterns);
   - seeded random patterns drawn like the batching workload (core from
     {edge, wedge, triangle, 4-path, 4-cycle, diamond, 4-clique, 5-cycle},
     0-12 fringes, each on a uniform random non-empty subset of the core).

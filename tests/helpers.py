@@ -6,7 +6,7 @@ import fsgc
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
-# the BASELINE workload patterns: (n, undirected edges)
+# the workload patterns (ER triangle + 2 fringes, and the eight RMAT patterns): (n, undirected edges)
 WORKLOAD = {
     "er_triangle_2fringes": (5, [(0, 1), (1, 2), (0, 2), (0, 3), (1, 4)]),
     "wedge_1_on_centre": (4, [(0, 1), (0, 2), (0, 3)]),
