@@ -196,9 +196,9 @@ bool mo_valid(const fsgc_matching_order& mo) {
 
 // The divisor for cores of 3+ vertices: the pattern counted in itself with the
 // same kernels.  The reference stores it in an int (src/fringeCount.cu:2213).
-int automorphisms(fsgc_ctx* c, const fsgc_matching_order& mo, u64* out) {
+int automorphisms(fsgc_ctx* c, const fsgc_matching_order& mo, u64* out, int exact_placements) {
   std::string key(reinterpret_cast<const char*>(&mo), sizeof(mo));
-  key.push_back(c->exact_placements ? 'x' : 'r');
+  key.push_back(exact_placements ? 'x' : 'r');
   auto it = c->aut_cache.find(key);
   if (it != c->aut_cache.end()) {
     *out = it->second;
@@ -214,7 +214,7 @@ int automorphisms(fsgc_ctx* c, const fsgc_matching_order& mo, u64* out) {
   st = ensure_slots(c, 1);
   if (st != FSGC_OK) { free_graph(pg); return st; }
   cudaMemsetAsync(c->d_slots, 0, sizeof(u64), c->stream);
-  fsgc::CountJob job{&mo, pg, c->d_slots, 0, 0, false, c->exact_placements, nullptr, 1};
+  fsgc::CountJob job{&mo, pg, c->d_slots, 0, 0, false, exact_placements, nullptr, 1};
   st = fsgc::enqueue_count(job, c->stream, &c->launches, c->work);
   u64 raw = 0;
   if (st == FSGC_OK) {
@@ -265,7 +265,7 @@ int plan_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, std::vector<u64>& au
     if (!g) return fail(c, FSGC_ENOTFOUND, "task %d: unknown graph %d", t, tasks[t].gid);
     if (g->ngraphs > 0) return fail(c, FSGC_EINVAL, "task %d: graph %d is packed; use fsgc_count_packed", t, tasks[t].gid);
     if (mo.nodes >= 3 && !pattern_too_large(mo, *g)) {
-      const int st = automorphisms(c, mo, &aut[(size_t)t]);
+      const int st = automorphisms(c, mo, &aut[(size_t)t], c->exact_placements);
       if (st != FSGC_OK) return st;
     }
   }
@@ -589,7 +589,7 @@ int fsgc_count_packed(fsgc_ctx* c, int gid, const fsgc_matching_order* mo, fsgc_
   for (int i = 0; i < ng; i++) any_fits = any_fits || !(pn > g->member_n[i] || pm > g->member_m[i]);
   u64 aut = 1;
   if (mo->nodes >= 3 && any_fits) {
-    const int st = automorphisms(c, *mo, &aut);
+    const int st = automorphisms(c, *mo, &aut, c->exact_placements);
     if (st != FSGC_OK) return st;
   }
   if (ng > c->member_cap) {
@@ -666,6 +666,70 @@ int fsgc_graph_info_get(fsgc_ctx* c, int gid, fsgc_graph_info* out) {
   out->max_degree = g->maxdeg;
   out->triangles = g->prepared ? g->triangles : -1;
   out->device_bytes = (int64_t)g->bytes;
+  return FSGC_OK;
+}
+
+int fsgc_count_exact(fsgc_ctx* c, int gid, const fsgc_matching_order* mo, fsgc_exact_result* out) {
+  if (!c || !mo || !out) return fail(c, FSGC_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  memset(out, 0, sizeof(*out));
+  if (!mo_valid(*mo)) return fail(c, FSGC_EINVAL, "malformed matching order");
+  DevGraph* g = find_graph(c, gid);
+  if (!g) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", gid);
+  if (g->ngraphs > 0) return fail(c, FSGC_EUNSUPPORTED, "exact counts of packed graphs are not supported");
+  if (pattern_too_large(*mo, *g)) {
+    out->flags = FSGC_FLAG_PATTERN_TOO_LARGE;
+    out->core_type = (mo->nodes == 3) ? ((__builtin_popcount(mo->list[1]) == 1) ? FSGC_CORE_WEDGE : FSGC_CORE_TRIANGLE)
+                                      : FSGC_CORE_GENERAL;
+    return FSGC_OK;
+  }
+  // the divisor is the pattern counted in itself with exact placements (small, exact in u64)
+  u64 aut = 1;
+  int st = FSGC_OK;
+  if (mo->nodes >= 3) {
+    st = automorphisms(c, *mo, &aut, 1);
+    if (st != FSGC_OK) return st;
+  }
+  st = ensure_slots(c, 3);
+  if (st != FSGC_OK) return st;
+  st = ensure_events(c, 2);
+  if (st != FSGC_OK) return st;
+  CK(cudaMemsetAsync(c->d_slots, 0, 3 * sizeof(u64), c->stream), "slot reset");
+  CK(cudaEventRecord(c->events[0], c->stream), "event");
+  fsgc::CountJob job{mo, g, c->d_slots, 0, 0, false, 1, nullptr, 1};
+  job.exact_count = true;
+  st = fsgc::enqueue_count(job, c->stream, &c->launches, c->work);
+  if (st != FSGC_OK) {
+    cudaStreamSynchronize(c->stream);
+    return fail(c, st, "exact count failed (%s)", cudaGetErrorString(cudaGetLastError()));
+  }
+  CK(cudaEventRecord(c->events[1], c->stream), "event");
+  CK(cudaMemcpyAsync(c->h_slots, c->d_slots, 3 * sizeof(u64), cudaMemcpyDeviceToHost, c->stream), "readback");
+  CK(cudaStreamSynchronize(c->stream), "exact count");
+  unsigned __int128 raw;
+  bool sat = false;
+  if (job.host_only) {
+    raw = job.host_value;
+  } else {
+    raw = ((unsigned __int128)c->h_slots[1] << 64) | c->h_slots[0];
+    sat = c->h_slots[2] != 0 || raw == ~(unsigned __int128)0;
+  }
+  out->core_type = job.core_type;
+  out->automorphisms = aut;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->events[0], c->events[1]);
+  out->device_ms = ms;
+  if (sat) {
+    out->flags |= FSGC_FLAG_SATURATED;
+    out->raw_lo = out->raw_hi = out->count_lo = out->count_hi = ~0ULL;
+    return FSGC_OK;
+  }
+  const unsigned __int128 q = raw / aut;
+  out->raw_lo = (u64)raw;
+  out->raw_hi = (u64)(raw >> 64);
+  out->count_lo = (u64)q;
+  out->count_hi = (u64)(q >> 64);
   return FSGC_OK;
 }
 

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "fsgc_internal.h"
@@ -44,12 +45,22 @@ enum { IU = 1, IV = 2, IW = 4, IUV = 3, IUW = 5, IVW = 6, IUVW = 7 };
 
 __device__ __forceinline__ u64 nck(int n, int k) { return nck_ref(n, k, c_div); }
 
+// Arithmetic of a count: u64 with the reference's wrapping binomials (A = u64),
+// or exact saturating 128-bit values (A = X128).
+template <class A> __device__ __forceinline__ A nck_a(int n, int k);
+template <> __device__ __forceinline__ u64 nck_a<u64>(int n, int k) { return nck(n, k); }
+template <> __device__ __forceinline__ X128 nck_a<X128>(int n, int k) { return nck_x(n, k); }
+__device__ __forceinline__ bool a_is_zero(u64 x) { return x == 0; }
+__device__ __forceinline__ bool a_is_zero(const X128& x) { return x.is_zero(); }
+
 // Adds one match's value: into the thread's running sum for an ordinary graph,
 // into the result slot of the match's member graph for a packed graph.
 __device__ __forceinline__ void credit(const GView& g, u64& acc, u64 x, int vertex) {
   if (g.comp == nullptr) acc += x;
   else if (x) atomicAdd(g.comp_slots + g.comp[vertex], x);
 }
+// exact counts run on ordinary graphs only
+__device__ __forceinline__ void credit(const GView&, X128& acc, X128 x, int) { acc += x; }
 __device__ __forceinline__ int relabel_of(const GView& g, int relabel, int vertex) {
   return g.comp ? (int)g.comp_relabel[g.comp[vertex]] : relabel;
 }
@@ -57,79 +68,82 @@ __device__ __forceinline__ int relabel_of(const GView& g, int relabel, int verte
 // ------------------------------------------------------------- shared formulas
 // Edge-core formula (src/fringeCount.cu:2030-2049) for an edge (u, v), where
 // u is the endpoint with the larger vertex id and c_uv = |N(u) & N(v)|.
-__device__ u64 edge_formula(int du, int dv, int c_uv, int f_u, int f_uv, int f_v) {
+template <class A>
+__device__ A edge_formula(int du, int dv, int c_uv, int f_u, int f_uv, int f_v) {
   const int a_uv = c_uv - f_uv;
   if (a_uv < 0) return 0;
   const int c_u = du - 1 - c_uv, c_v = dv - 1 - c_uv;
   const int bound = min(f_u, a_uv);
-  u64 acc = 0;
+  A acc = 0;
   for (int j = 0; j <= bound; j++) {
     const int k = f_u - j;
-    u64 term = nck(c_u, k) * nck(a_uv + c_v - j, f_v);
-    if (f_u != f_v) term += nck(c_v, k) * nck(a_uv + c_u - j, f_v);
-    acc += term * nck(a_uv, j);
+    A term = nck_a<A>(c_u, k) * nck_a<A>(a_uv + c_v - j, f_v);
+    if (f_u != f_v) term += nck_a<A>(c_v, k) * nck_a<A>(a_uv + c_u - j, f_v);
+    acc += term * nck_a<A>(a_uv, j);
   }
-  return acc * nck(c_uv, f_uv);
+  return acc * nck_a<A>(c_uv, f_uv);
 }
 
 // wedge() (src/fringeCount.cu:1381-1406): endpoints x (larger id) and y of a
 // wedge; c = common neighbours of x and y other than the centre.
-__device__ u64 wedge_formula(int dx, int dy, bool adj, int f_x, int f_xy, int f_y, int c) {
+template <class A>
+__device__ A wedge_formula(int dx, int dy, bool adj, int f_x, int f_xy, int f_y, int c) {
   const int a_xy = c - f_xy;
   if (a_xy < 0) return 0;
   const int corr = adj ? 2 : 1;
   const int a_x = dx - (corr + c), a_y = dy - (corr + c);
   const int bound = min(f_x, a_xy);
-  u64 sum = 0;
+  A sum = 0;
   for (int j = 0; j <= bound; j++) {
     const int k = f_x - j;
-    u64 term = nck(a_x, k) * nck(a_xy + a_y - j, f_y);
-    if (f_x != f_y) term += nck(a_y, k) * nck(a_xy + a_x - j, f_y);
-    sum += term * nck(a_xy, j);
+    A term = nck_a<A>(a_x, k) * nck_a<A>(a_xy + a_y - j, f_y);
+    if (f_x != f_y) term += nck_a<A>(a_y, k) * nck_a<A>(a_xy + a_x - j, f_y);
+    sum += term * nck_a<A>(a_xy, j);
   }
-  return sum * nck(c, f_xy);
+  return sum * nck_a<A>(c, f_xy);
 }
 
 // fc3 (src/fringeCount.cu:233-327): placements of the seven anchor-set types of
 // a 3-vertex core into its seven exclusive Venn regions.  Same summation
 // indices and the same nck factors per term as the reference.
-__device__ u64 fc3(const int* fr, const int* venn) {
+template <class A>
+__device__ A fc3(const int* fr, const int* venn) {
   const int fuvw = fr[IUVW], fuv = fr[IUV], fuw = fr[IUW], fvw = fr[IVW];
   const int fu = fr[IU], fv = fr[IV], fw = fr[IW];
   int x_uvw = venn[IUVW];
   const int x_uv = venn[IUV], x_uw = venn[IUW], x_vw = venn[IVW];
   const int x_u = venn[IU], x_v = venn[IV], x_w = venn[IW];
   if (x_uvw < fuvw) return 0;
-  const u64 base = nck(x_uvw, fuvw);
+  const A base = nck_a<A>(x_uvw, fuvw);
   x_uvw -= fuvw;
-  u64 total = 0;
+  A total = 0;
   for (int i = min(x_uvw, fuv); i >= 0; i--) {
     if (x_uv < fuv - i) break;
-    const u64 t1 = base * nck(x_uvw, i) * nck(x_uv, fuv - i);
+    const A t1 = base * nck_a<A>(x_uvw, i) * nck_a<A>(x_uv, fuv - i);
     const int r1 = x_uvw - i, r_uv = x_uv - (fuv - i);
     for (int j = min(r1, fuw); j >= 0; j--) {
       if (x_uw < fuw - j) break;
-      const u64 t2 = t1 * nck(r1, j) * nck(x_uw, fuw - j);
+      const A t2 = t1 * nck_a<A>(r1, j) * nck_a<A>(x_uw, fuw - j);
       const int r2 = r1 - j, r_uw = x_uw - (fuw - j);
       for (int k = min(r2, fvw); k >= 0; k--) {
         if (x_vw < fvw - k) break;
-        const u64 t3 = t2 * nck(r2, k) * nck(x_vw, fvw - k);
+        const A t3 = t2 * nck_a<A>(r2, k) * nck_a<A>(x_vw, fvw - k);
         const int r3 = r2 - k, r_vw = x_vw - (fvw - k);
         for (int a = min(r3, fu); a >= 0; a--) {
-          const u64 ta = t3 * nck(r3, a);
+          const A ta = t3 * nck_a<A>(r3, a);
           const int pool_v = (r3 - a) + r_vw;
           for (int b = min(r_uv, fu - a); b >= 0; b--) {
-            const u64 tb = ta * nck(r_uv, b);
+            const A tb = ta * nck_a<A>(r_uv, b);
             const int r_uv2 = r_uv - b;
             for (int c = min(r_uw, fu - a - b); c >= 0; c--) {
               if (x_u < fu - a - b - c) break;
-              const u64 tc = tb * nck(r_uw, c) * nck(x_u, fu - a - b - c);
+              const A tc = tb * nck_a<A>(r_uw, c) * nck_a<A>(x_u, fu - a - b - c);
               const int r_uw2 = r_uw - c;
               for (int d = min(pool_v, fv); d >= 0; d--) {
                 if (r_uv2 + x_v < fv - d) break;
-                const u64 td = tc * nck(pool_v, d) * nck(r_uv2 + x_v, fv - d);
+                const A td = tc * nck_a<A>(pool_v, d) * nck_a<A>(r_uv2 + x_v, fv - d);
                 const int pool_w = (pool_v - d) + r_uw2 + x_w;
-                if (pool_w >= fw) total += td * nck(pool_w, fw);
+                if (pool_w >= fw) total += td * nck_a<A>(pool_w, fw);
               }
             }
           }
@@ -146,11 +160,12 @@ struct Rot3 {
 };
 
 // ------------------------------------------------------------- vertex core
+template <class A>
 __global__ void star_kernel(GView g, int t, u64* __restrict__ slot) {
-  u64 acc = 0;
+  A acc = A(0);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x) {
     const int d = g.deg[v];
-    if (d >= t) credit(g, acc, nck(d, t), v);
+    if (d >= t) credit(g, acc, nck_a<A>(d, t), v);
   }
   block_sum_to(acc, slot);
 }
@@ -160,26 +175,28 @@ struct EdgeParams {
   int f_u, f_uv, f_v, lim1, lim2;
 };
 
+template <class A>
 __global__ void edge_kernel(GView g, EdgeParams p, u64* __restrict__ slot) {
   const long long me = g.m / 2;
-  u64 acc = 0;
+  A acc = A(0);
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < me; j += (long long)gridDim.x * blockDim.x) {
     const int a = g.osrc[j], b = g.oadj[j];
     const int u = max(a, b), v = min(a, b);  // the reference orients by id, v < u
     const int du = g.deg[u], dv = g.deg[v];
     if (!(du > p.lim1 && dv > p.lim1 && du + dv > p.lim2)) continue;  // init_wl_edge pruning
-    credit(g, acc, edge_formula(du, dv, (int)g.osup[j], p.f_u, p.f_uv, p.f_v), a);
+    credit(g, acc, edge_formula<A>(du, dv, (int)g.osup[j], p.f_u, p.f_uv, p.f_v), a);
   }
   block_sum_to(acc, slot);
 }
 
 // triangle with `tails` fringes on one vertex: sum over triangles of the three
 // vertex terms = sum over vertices of (triangles at v) * C(deg v - 2, tails)
+template <class A>
 __global__ void tailed_triangle_kernel(GView g, const u64* __restrict__ vtri2, int tails, u64* __restrict__ slot) {
-  u64 acc = 0;
+  A acc = A(0);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x) {
     const u64 t2 = vtri2[v];
-    if (t2) credit(g, acc, (t2 >> 1) * nck(g.deg[v] - 2, tails), v);
+    if (t2) credit(g, acc, A(t2 >> 1) * nck_a<A>(g.deg[v] - 2, tails), v);
   }
   block_sum_to(acc, slot);
 }
@@ -235,11 +252,12 @@ __device__ __forceinline__ long long tri_key(int x, int d, int relabel) {
 
 // One lane per oriented edge (a -> b); triangles a < b < c are found by merging
 // the out-lists.  Found triangles are served one at a time by the whole warp.
+template <class Ar>  // (A and B name out-lists below)
 __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slot) {
   const int lane = threadIdx.x & 31;
   const long long me = g.m / 2;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  u64 acc = 0;
+  Ar acc = Ar(0);
   for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x - lane); base < me; base += nwarps * 32) {
     const long long j = base + lane;
     bool live = j < me;
@@ -273,9 +291,9 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
           for (int t = 0; t < lc; t++) {
             const int d = __ldg(C + t);
             if (bsearch_has(A, la, d) && bsearch_has(B, lb, d)) {
-              if (p.mode == 1) credit(g, acc, 1, a);
-              else credit(g, acc, nck(g.deg[a] - 3, p.tails) + nck(g.deg[b] - 3, p.tails) + nck(g.deg[c] - 3, p.tails) +
-                                  nck(g.deg[d] - 3, p.tails), a);
+              if (p.mode == 1) credit(g, acc, Ar(1), a);
+              else credit(g, acc, nck_a<Ar>(g.deg[a] - 3, p.tails) + nck_a<Ar>(g.deg[b] - 3, p.tails) +
+                                  nck_a<Ar>(g.deg[c] - 3, p.tails) + nck_a<Ar>(g.deg[d] - 3, p.tails), a);
             }
           }
         }
@@ -339,8 +357,8 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
           venn[IV] = dv - (c12 + c23 + (c123 + 2));
           venn[IW] = dw - (c13 + c23 + (c123 + 2));
           venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
-          u64 t = 0;
-          for (int r = 0; r < p.rot.count; r++) t += fc3(p.rot.fr[r], venn);
+          Ar t = Ar(0);
+          for (int r = 0; r < p.rot.count; r++) t += fc3<Ar>(p.rot.fr[r], venn);
           credit(g, acc, t, a);
         }
       }
@@ -357,6 +375,7 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
 // iff bit pos(b_j) of M_i is set, |N(a) & N(b_i)| = popc(M_i), and the triple
 // overlap |N(a) & N(b_i) & N(b_j)| = popc(M_i & M_j) -- a few word operations
 // per triangle instead of an intersection of full neighbour lists.
+template <class A>
 __global__ void __launch_bounds__(256, 3) triangle_bitmap_kernel(GView g, TriParams p, int* __restrict__ queue,
                                                               unsigned* __restrict__ bits_all, long long bits_per_block,
                                                               u64* __restrict__ slot) {
@@ -368,7 +387,7 @@ __global__ void __launch_bounds__(256, 3) triangle_bitmap_kernel(GView g, TriPar
   int* outl = s_dyn;            // out-neighbours of a
   int* pos = s_dyn + kmax;      // their positions in N(a)
   int* rowpop = s_dyn + 2 * kmax;  // |N(a) & N(b_i)|
-  u64 acc = 0;
+  A acc = A(0);
   for (;;) {
     if (threadIdx.x == 0) s_a = atomicAdd(queue, 1);
     __syncthreads();
@@ -451,8 +470,8 @@ __global__ void __launch_bounds__(256, 3) triangle_bitmap_kernel(GView g, TriPar
           venn[IV] = dv - (c12 + c23 + (c123 + 2));
           venn[IW] = dw - (c13 + c23 + (c123 + 2));
           venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
-          u64 t = 0;
-          for (int r = 0; r < p.rot.count; r++) t += fc3(p.rot.fr[r], venn);
+          A t = A(0);
+          for (int r = 0; r < p.rot.count; r++) t += fc3<A>(p.rot.fr[r], venn);
           credit(g, acc, t, a);
         }
       }
@@ -580,16 +599,16 @@ __device__ void block_scan_inplace(int* x, int n, WedgeSmem<BIG>& S) {
   if (tid == 0) x[n] = carry;
 }
 
-template <bool BIG>
+template <bool BIG, class A>
 __device__ __forceinline__ void eval_pair(const GView& g, const WedgeParams& p, WedgeSmem<BIG>& S, int lo, int o,
-                                          unsigned C, int dw, int v, int dv, int thres, u64& acc) {
+                                          unsigned C, int dw, int v, int dv, int thres, A& acc) {
   if (dw >= thres) {
     const bool vw = (S.adjbits[o >> 5] >> (o & 31)) & 1u;
-    credit(g, acc, (u64)C * wedge_formula(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1), v);
+    credit(g, acc, A((u64)C) * wedge_formula<A>(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1), v);
   }
 }
 
-template <bool BIG>
+template <bool BIG, class A>
 __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, WedgeParams p, int* __restrict__ queue,
                                                                    long long* __restrict__ gcur, int* __restrict__ gpre,
                                                                    long long gstride, ChunkTable tab,
@@ -605,7 +624,7 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
   for (int i = tid; i < WORDS; i += blockDim.x) S.cnt[i] = 0;
   for (int i = tid; i < TW; i += blockDim.x) S.touched[i] = 0;
   for (int i = tid; i < WedgeCfg<BIG>::CH_MAX / 32; i += blockDim.x) S.adjbits[i] = 0;
-  u64 acc = 0;
+  A acc = A(0);
   for (;;) {
     if (tid == 0) {
       S.v = atomicAdd(queue, 1);
@@ -730,7 +749,7 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
             S.cnt[wd] = 0;
             if (BIG) {
               const int w = lo + wd;
-              eval_pair<BIG>(g, p, S, lo, wd, word, g.deg[w], v, dv, thres, acc);
+              eval_pair<BIG, A>(g, p, S, lo, wd, word, g.deg[w], v, dv, thres, acc);
             } else {
               const int o0 = wd << lper;
               const unsigned cmask = (bits == 16) ? 0xffffu : ((1u << bits) - 1);
@@ -738,7 +757,7 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
                 const int k = (__ffs(rest) - 1) / bits;  // next non-zero counter of the word
                 const unsigned C = (word >> (k * bits)) & cmask;
                 rest &= ~(cmask << (k * bits));
-                eval_pair<BIG>(g, p, S, lo, o0 + k, C, g.deg[lo + o0 + k], v, dv, thres, acc);
+                eval_pair<BIG, A>(g, p, S, lo, o0 + k, C, g.deg[lo + o0 + k], v, dv, thres, acc);
               }
             }
           }
@@ -798,12 +817,13 @@ struct GWedgeParams {
 // warp per centre u, looping over endpoints v in N(u); lanes take w in N(u),
 // w < v; open wedges use rotations 0 (and 3), triangles (counted once, with
 // u < w < v) use all rotations.
+template <class A>
 __global__ void wedge_general_kernel(GView g, GWedgeParams p, const unsigned* __restrict__ esup,
                                      u64* __restrict__ slot) {
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  u64 acc = 0;
+  A acc = A(0);
   // one warp per list entry (u, v): a hub centre's pairs spread over as many
   // warps as it has neighbours
   for (long long j = wid; j < g.m; j += nw) {
@@ -878,14 +898,14 @@ __global__ void wedge_general_kernel(GView g, GWedgeParams p, const unsigned* __
           venn[IV] = dv - (p12 + c23);
           venn[IW] = dw - (c13 + c23 + c123);
           venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
-          u64 t = 0;
+          A t = A(0);
           if (tri) {
             venn[IUV]--; venn[IUW]--; venn[IVW]--;
-            for (int r = 0; r < p.rot.count; r++) t += fc3(p.rot.fr[r], venn);
+            for (int r = 0; r < p.rot.count; r++) t += fc3<A>(p.rot.fr[r], venn);
           } else {
             venn[IU] -= 2; venn[IVW]--;
-            t += fc3(p.rot.fr[0], venn);
-            if (p.rot.count > 3) t += fc3(p.rot.fr[3], venn);
+            t += fc3<A>(p.rot.fr[0], venn);
+            if (p.rot.count > 3) t += fc3<A>(p.rot.fr[3], venn);
           }
           credit(g, acc, t, u);
         }
@@ -919,15 +939,16 @@ struct GenParams {
 // step list: step s puts a fringes of its anchor set into region slot_idx[s];
 // the last step of each set takes all its remaining fringes.  Each complete
 // placement adds the product of nck(remaining region size, fringes placed).
-__device__ u64 placement_sum(const GenParams& p, int* venn) {
+template <class A>
+__device__ A placement_sum(const GenParams& p, int* venn) {
   int a_[kMaxSlots];
   int rem_[kMaxSlots];
-  u64 pre_[kMaxSlots];
+  A pre_[kMaxSlots];
   const int S = p.nslots;
-  u64 sum = 0;
+  A sum = A(0);
   int s = 0;
   rem_[0] = p.fcnt[p.slot_set[0]];
-  pre_[0] = 1;
+  pre_[0] = A(1);
   a_[0] = p.slot_top[0] ? rem_[0] : min(venn[p.slot_idx[0]], rem_[0]);
   while (s >= 0) {
     if (a_[s] < 0) {  // this step is exhausted: back up
@@ -939,8 +960,8 @@ __device__ u64 placement_sum(const GenParams& p, int* venn) {
       continue;
     }
     const int idx = p.slot_idx[s];
-    const u64 w = pre_[s] * nck(venn[idx], a_[s]);
-    if (w == 0 || s == S - 1) {
+    const A w = pre_[s] * nck_a<A>(venn[idx], a_[s]);
+    if (a_is_zero(w) || s == S - 1) {
       sum += w;
       a_[s] = p.slot_top[s] ? -1 : a_[s] - 1;
       continue;
@@ -1063,8 +1084,8 @@ __device__ void venn_general(const GView& g, const GenParams& p, const int* stac
   (void)top;
 }
 
-template <int L>
-__device__ u64 gen_level(const GView& g, const GenParams& p, GenWarp& w) {
+template <int L, class A>
+__device__ A gen_level(const GView& g, const GenParams& p, GenWarp& w) {
   // choose stack[L+1] among the neighbours of the first core vertex it must touch
   const int lane = threadIdx.x & 31;
   const int list = p.list[L];
@@ -1073,7 +1094,7 @@ __device__ u64 gen_level(const GView& g, const GenParams& p, GenWarp& w) {
   const long long sb = g.off[src];
   const int sd = (int)(g.off[src + 1] - sb);
   const bool last = (L + 1 == p.k - 1);
-  u64 acc = 0;
+  A acc = A(0);
   for (int t0 = 0; t0 < sd; t0 += 32) {
     const int t = t0 + lane;
     bool ok = false;
@@ -1105,8 +1126,13 @@ __device__ u64 gen_level(const GView& g, const GenParams& p, GenWarp& w) {
         venn_general(g, p, w.stack, w.venn[who]);
       }
       __syncwarp();
-      if (ok) credit(g, acc, p.exact ? placement_sum(p, w.venn[lane]) : placement_sum_reference(p, w.venn[lane]),
-                     w.stack[0]);
+      if (ok) {
+        if constexpr (std::is_same<A, u64>::value)
+          credit(g, acc, p.exact ? placement_sum<u64>(p, w.venn[lane]) : placement_sum_reference(p, w.venn[lane]),
+                 w.stack[0]);
+        else
+          credit(g, acc, placement_sum<A>(p, w.venn[lane]), w.stack[0]);  // exact counts: exact placements
+      }
       __syncwarp();
     } else {
       while (bal) {
@@ -1115,7 +1141,7 @@ __device__ u64 gen_level(const GView& g, const GenParams& p, GenWarp& w) {
         const int xx = __shfl_sync(0xffffffffu, x, who);
         if (lane == 0) w.stack[L + 1] = xx;
         __syncwarp();
-        if constexpr (L < 4) acc += gen_level<L + 1>(g, p, w);
+        if constexpr (L < 4) acc += gen_level<L + 1, A>(g, p, w);
       }
     }
   }
@@ -1123,12 +1149,13 @@ __device__ u64 gen_level(const GView& g, const GenParams& p, GenWarp& w) {
 }
 
 // one warp per directed edge (u, v): u = core vertex A, v = core vertex B
+template <class A>
 __global__ void __launch_bounds__(kGenWarps * 32) general_core_kernel(GView g, const __grid_constant__ GenParams p,
                                                                        int* __restrict__ queue, u64* __restrict__ slot) {
   __shared__ GenWarp sw[kGenWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   GenWarp& w = sw[warp];
-  u64 acc = 0;
+  A acc = A(0);
   for (;;) {
     int u = 0;
     if (lane == 0) u = atomicAdd(queue, 1);
@@ -1142,7 +1169,7 @@ __global__ void __launch_bounds__(kGenWarps * 32) general_core_kernel(GView g, c
       if (g.deg[v] < p.destdeg[0]) continue;  // init_wl_general
       if (lane == 0) { w.stack[0] = u; w.stack[1] = v; }
       __syncwarp();
-      acc += gen_level<1>(g, p, w);
+      acc += gen_level<1, A>(g, p, w);
       __syncwarp();
     }
   }
@@ -1331,7 +1358,9 @@ int prepare_for_count(const fsgc_matching_order& mo, DevGraph& G, cudaStream_t s
   return cudaStreamSynchronize(s) == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }
 
-int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work) {
+namespace {
+template <class A>
+int enqueue_count_a(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work) {
   const fsgc_matching_order& mo = *job.mo;
   DevGraph& G = *job.g;
   job.host_only = false;
@@ -1349,7 +1378,7 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
     if (mo.fcnt[0] == 1) { job.host_only = true; job.host_value = (u64)(G.m / 2); return FSGC_OK; }
     GView gv0 = G.view();
     gv0.comp_slots = job.d_comp_slots;
-    star_kernel<<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(gv0, mo.fcnt[0], job.d_slot);
+    star_kernel<A><<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(gv0, mo.fcnt[0], job.d_slot);
     *launches += 1;
     return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
   }
@@ -1383,13 +1412,13 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
       }
       st = ensure_vertex_triangles(G, s, launches);
       if (st != FSGC_OK) return st;
-      tailed_triangle_kernel<<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(gv, G.vtri2, f_v, job.d_slot);
+      tailed_triangle_kernel<A><<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(gv, G.vtri2, f_v, job.d_slot);
       *launches += 1;
       return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
     }
     EdgeParams ep{f_u, f_uv, f_v, f_u + f_uv, f_u + f_uv + f_v};
     if (me > 0) {
-      edge_kernel<<<grid_for(me, TPB, 8), TPB, 0, s>>>(gv, ep, job.d_slot);
+      edge_kernel<A><<<grid_for(me, TPB, 8), TPB, 0, s>>>(gv, ep, job.d_slot);
       *launches += 1;
     }
     return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
@@ -1424,8 +1453,8 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
       const int blocks = sm_count();
       {
         const size_t smem = sizeof(WedgeSmem<false>);
-        cudaFuncSetAttribute(wedge_chunk_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        wedge_chunk_kernel<false><<<blocks, kWThreads, smem, s>>>(gv, wp, q1, nullptr, nullptr, 0, tab, job.d_slot);
+        cudaFuncSetAttribute(wedge_chunk_kernel<false, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        wedge_chunk_kernel<false, A><<<blocks, kWThreads, smem, s>>>(gv, wp, q1, nullptr, nullptr, 0, tab, job.d_slot);
         *launches += 1;
       }
       if (G.maxdeg > kWDvMax) {
@@ -1437,8 +1466,8 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
         long long* gcur = reinterpret_cast<long long*>(work.tri.ptr);
         int* gpre = reinterpret_cast<int*>(gcur + (size_t)blocks * 2 * gs);
         const size_t smem = sizeof(WedgeSmem<true>);
-        cudaFuncSetAttribute(wedge_chunk_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        wedge_chunk_kernel<true><<<blocks, kWThreads, smem, s>>>(gv, wp, q2, gcur, gpre, gs, tab, job.d_slot);
+        cudaFuncSetAttribute(wedge_chunk_kernel<true, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        wedge_chunk_kernel<true, A><<<blocks, kWThreads, smem, s>>>(gv, wp, q2, gcur, gpre, gs, tab, job.d_slot);
         *launches += 1;
       }
       return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
@@ -1448,7 +1477,7 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
     rotations3(f, true, gp.rot);
     st = ensure_entry_supports(G, s, launches);
     if (st != FSGC_OK) return st;
-    wedge_general_kernel<<<grid_for(G.m * 32, TPB, 8), TPB, 0, s>>>(gv, gp, G.esup, job.d_slot);
+    wedge_general_kernel<A><<<grid_for(G.m * 32, TPB, 8), TPB, 0, s>>>(gv, gp, G.esup, job.d_slot);
     *launches += 1;
     return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
   }
@@ -1482,11 +1511,11 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
       int* queue = reinterpret_cast<int*>(work.small + 6);
       cudaMemsetAsync(queue, 0, sizeof(int), s);
       if (smem > 48 * 1024)
-        cudaFuncSetAttribute(triangle_bitmap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      triangle_bitmap_kernel<<<blocks, 256, smem, s>>>(gv, tp, queue, reinterpret_cast<unsigned*>(work.tri.ptr),
+        cudaFuncSetAttribute(triangle_bitmap_kernel<A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      triangle_bitmap_kernel<A><<<blocks, 256, smem, s>>>(gv, tp, queue, reinterpret_cast<unsigned*>(work.tri.ptr),
                                                         per_block, job.d_slot);
     } else {
-      triangle_core_kernel<<<grid_for(me, TPB, 8), TPB, 0, s>>>(gv, tp, job.d_slot);
+      triangle_core_kernel<A><<<grid_for(me, TPB, 8), TPB, 0, s>>>(gv, tp, job.d_slot);
     }
     *launches += 1;
     return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
@@ -1526,10 +1555,15 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
   int* queue = reinterpret_cast<int*>(work.small + 5);
   cudaMemsetAsync(queue, 0, sizeof(int), s);
   const int blocks = sm_count() * 8;
-  general_core_kernel<<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
+  general_core_kernel<A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
   *launches += 1;
   delete gp;
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+}  // namespace
+
+int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work) {
+  return job.exact_count ? enqueue_count_a<X128>(job, s, launches, work) : enqueue_count_a<u64>(job, s, launches, work);
 }
 
 // Launchers for callers that bring their own device memory (noalloc.cu): the
@@ -1538,8 +1572,8 @@ int launch_wedge_small(const GView& gv, int f_v, int f_vw, int f_w, int lim, int
                        cudaStream_t s) {
   WedgeParams wp{f_v, f_vw, f_w, lim, minsum};
   const size_t smem = sizeof(WedgeSmem<false>);
-  cudaFuncSetAttribute(wedge_chunk_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  wedge_chunk_kernel<false><<<sm_count(), kWThreads, smem, s>>>(gv, wp, queue, nullptr, nullptr, 0,
+  cudaFuncSetAttribute(wedge_chunk_kernel<false, u64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  wedge_chunk_kernel<false, u64><<<sm_count(), kWThreads, smem, s>>>(gv, wp, queue, nullptr, nullptr, 0,
                                                                 ChunkTable{nullptr, nullptr, 0}, slot);
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }
@@ -1548,8 +1582,8 @@ int launch_wedge_big(const GView& gv, int f_v, int f_vw, int f_w, int lim, int m
                      int* gpre, long long gstride, int blocks, u64* slot, cudaStream_t s) {
   WedgeParams wp{f_v, f_vw, f_w, lim, minsum};
   const size_t smem = sizeof(WedgeSmem<true>);
-  cudaFuncSetAttribute(wedge_chunk_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  wedge_chunk_kernel<true><<<blocks, kWThreads, smem, s>>>(gv, wp, queue, gcur, gpre, gstride,
+  cudaFuncSetAttribute(wedge_chunk_kernel<true, u64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  wedge_chunk_kernel<true, u64><<<blocks, kWThreads, smem, s>>>(gv, wp, queue, gcur, gpre, gstride,
                                                            ChunkTable{nullptr, nullptr, 0}, slot);
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }

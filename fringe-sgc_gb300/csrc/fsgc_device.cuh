@@ -103,6 +103,82 @@ __device__ __forceinline__ int lower_bound_dev(const int* __restrict__ a, int le
 }
 
 // ----------------------------------------------------------------------------
+// Exact counts: unsigned 128-bit values that saturate at 2^128 - 1 (every bit
+// set) instead of wrapping.  A product with a zero factor is zero; any other
+// operation with a saturated operand, or whose true result is >= 2^128 - 1,
+// gives the saturated value.  Used where the reference's u64 arithmetic wraps.
+struct X128 {
+  u64 lo, hi;
+  __host__ __device__ X128() : lo(0), hi(0) {}
+  __host__ __device__ X128(u64 x) : lo(x), hi(0) {}
+  __host__ __device__ X128(u64 l, u64 h) : lo(l), hi(h) {}
+  __host__ __device__ static X128 saturated() { return X128(~0ULL, ~0ULL); }
+  __host__ __device__ bool is_saturated() const { return (lo & hi) == ~0ULL; }
+  __host__ __device__ bool is_zero() const { return (lo | hi) == 0; }
+};
+
+__host__ __device__ inline X128 operator+(X128 a, X128 b) {
+  if (a.is_saturated() || b.is_saturated()) return X128::saturated();
+  X128 r;
+  r.lo = a.lo + b.lo;
+  const u64 c = r.lo < a.lo;
+  const u64 h = a.hi + b.hi;
+  r.hi = h + c;
+  if (h < a.hi || r.hi < h || r.is_saturated()) return X128::saturated();
+  return r;
+}
+
+__host__ __device__ inline X128 operator*(X128 a, X128 b) {
+  if (a.is_zero() || b.is_zero()) return X128();
+  if (a.is_saturated() || b.is_saturated() || (a.hi && b.hi)) return X128::saturated();
+  // at most one high word is non-zero: a*b = lo*lo + 2^64 (a.hi*b.lo + a.lo*b.hi)
+  const u64 cross_a = a.hi ? a.hi : b.hi, cross_b = a.hi ? b.lo : a.lo;
+  if (mulhi64(cross_a, cross_b)) return X128::saturated();
+  const u64 cross = cross_a * cross_b;
+  X128 r;
+  r.lo = a.lo * b.lo;
+  const u64 h = mulhi64(a.lo, b.lo);
+  r.hi = h + cross;
+  if (r.hi < h || r.is_saturated()) return X128::saturated();
+  return r;
+}
+
+__host__ __device__ inline X128& operator+=(X128& a, X128 b) { return a = a + b; }
+__host__ __device__ inline X128& operator*=(X128& a, X128 b) { return a = a * b; }
+
+// a / d and a % d for 1 <= d < 2^32 (a not saturated), by 32-bit limbs.
+__host__ __device__ inline X128 x_divmod_small(X128 a, unsigned d, unsigned* rem) {
+  X128 q;
+  q.hi = a.hi / d;
+  u64 r = a.hi % d;
+  const u64 t1 = (r << 32) | (a.lo >> 32);
+  const u64 q1 = t1 / d;
+  r = t1 % d;
+  const u64 t0 = (r << 32) | (a.lo & 0xffffffffULL);
+  q.lo = (q1 << 32) | (t0 / d);
+  *rem = (unsigned)(t0 % d);
+  return q;
+}
+
+// Exact binomial C(n, k) (0 when k < 0 or n < k), saturating.  The step
+// r = r*(n+1-i)/i is taken as (r/i)*(n+1-i) + ((r%i)*(n+1-i))/i, exact because
+// i divides r*(n+1-i), so no intermediate exceeds the final C(n, i).
+__host__ __device__ inline X128 nck_x(int n, int k) {
+  if (k < 0 || n < k) return X128();
+  if (k > n - k) k = n - k;
+  if (k == 0) return X128(1);
+  X128 r((u64)n);
+  for (int i = 2; i <= k; i++) {
+    unsigned rem;
+    const X128 q = x_divmod_small(r, (unsigned)i, &rem);
+    const u64 f = (u64)(n + 1 - i);
+    r = q * X128(f) + X128(((u64)rem * f) / (u64)i);
+    if (r.is_saturated()) return r;
+  }
+  return r;
+}
+
+// ----------------------------------------------------------------------------
 // Reductions: warp shuffle -> one shared-memory atomic per warp -> one global
 // atomic per block into the task's result slot (mod 2^64 addition).
 __device__ __forceinline__ u64 warp_sum_u64(u64 v) {
@@ -121,6 +197,43 @@ __device__ __forceinline__ void block_sum_to(u64 v, u64* __restrict__ slot) {
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(&s_acc, v);
   __syncthreads();
   if (threadIdx.x == 0 && s_acc) atomicAdd(slot, s_acc);
+}
+
+// Exact sums: slot[0..1] = low and high words of a 128-bit total, slot[2] is
+// set to 1 once the total saturates.  Saturating adds within the warp, one
+// shared partial per warp summed by thread 0, then a 128-bit atomic add into
+// the slot: the low word's carry goes into the high word, and a carry out of
+// the high word saturates.  Every thread of the block must call this.
+__device__ __forceinline__ void block_sum_to(X128 v, u64* __restrict__ slot) {
+  __shared__ u64 s_part[32][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const X128 w(__shfl_down_sync(0xffffffffu, v.lo, o), __shfl_down_sync(0xffffffffu, v.hi, o));
+    v = v + w;
+  }
+  if (lane == 0) { s_part[warp][0] = v.lo; s_part[warp][1] = v.hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    X128 t;
+    for (int i = 0; i < (int)((blockDim.x + 31) >> 5); i++) t = t + X128(s_part[i][0], s_part[i][1]);
+    if (t.is_saturated()) {
+      atomicExch(slot + 2, 1ULL);
+    } else if (!t.is_zero()) {
+      const u64 old_lo = atomicAdd(slot, t.lo);
+      const u64 carry = (old_lo + t.lo < old_lo) ? 1ULL : 0ULL;
+      if (t.hi == ~0ULL && carry) {
+        atomicExch(slot + 2, 1ULL);
+      } else {
+        const u64 add_hi = t.hi + carry;
+        if (add_hi) {
+          const u64 old_hi = atomicAdd(slot + 1, add_hi);
+          if (old_hi + add_hi < old_hi) atomicExch(slot + 2, 1ULL);
+        }
+      }
+    }
+  }
+  __syncthreads();  // s_part is free again for a later call
 }
 
 }  // namespace fsgc

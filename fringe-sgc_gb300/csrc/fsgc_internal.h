@@ -113,6 +113,7 @@ struct CountJob {
   int exact_placements;  // general core: exact placement sum instead of the reference's
   u64* d_comp_slots;     // packed graphs: per-member result slots (zeroed by the caller)
   int per_member_div;    // packed graphs: divide each member's total by this on the host (1 = none)
+  bool exact_count = false;  // exact 128-bit sums: d_slot holds (lo, hi, saturated); ordinary graphs only
 };
 
 // Launchers over caller-provided device memory (used by noalloc.cu).

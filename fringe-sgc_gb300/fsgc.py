@@ -54,6 +54,24 @@ class GraphInfo(C.Structure):
                 ("device_bytes", C.c_int64)]
 
 
+class ExactResult(C.Structure):
+    _fields_ = [("count_lo", C.c_uint64), ("count_hi", C.c_uint64), ("raw_lo", C.c_uint64), ("raw_hi", C.c_uint64),
+                ("automorphisms", C.c_uint64), ("flags", C.c_uint32), ("core_type", C.c_int32),
+                ("device_ms", C.c_double)]
+
+    @property
+    def count(self):
+        return self.count_lo | (self.count_hi << 64)
+
+    @property
+    def raw_total(self):
+        return self.raw_lo | (self.raw_hi << 64)
+
+    @property
+    def saturated(self):
+        return bool(self.flags & 2)
+
+
 class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_uint64), ("rounds", C.c_uint64), ("queued", C.c_uint64),
                 ("in_use_bytes", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
@@ -102,6 +120,7 @@ def lib():
             "fsgc_graph_info_get": (I, [P, I, C.POINTER(GraphInfo)]),
             "fsgc_count": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(Result)]),
             "fsgc_count_batch": (I, [P, C.POINTER(Task), I, C.POINTER(Result)]),
+            "fsgc_count_exact": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(ExactResult)]),
             "fsgc_graph_from_packed_csr": (I, [P, I, I64, P, P, I, P, C.POINTER(C.c_int)]),
             "fsgc_count_packed": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(Result)]),
             "fsgc_ctx_timer_start": (I, [P]),
@@ -357,6 +376,12 @@ class Context:
         self._packed_sizes = getattr(self, "_packed_sizes", {})
         self._packed_sizes[gid.value] = len(graphs)
         return gid.value
+
+    def count_exact(self, gid, mo):
+        """Exact 128-bit count (ExactResult: .count, .raw_total, .saturated)."""
+        r = ExactResult()
+        _check(lib().fsgc_count_exact(self.ptr, gid, C.byref(mo), C.byref(r)), "count_exact", self.ptr)
+        return r
 
     def count_packed(self, gid, mo):
         ng = self._packed_sizes[gid]

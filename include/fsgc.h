@@ -174,6 +174,24 @@ int fsgc_count_packed(fsgc_ctx* ctx, int gid, const fsgc_matching_order* mo, fsg
 
 int fsgc_count(fsgc_ctx* ctx, int gid, const fsgc_matching_order* mo, fsgc_result* out);
 
+/* ---- exact counts (the reference has none: its u64 binomials wrap silently,
+ *      src/fringeCount.cu:189-197) ----
+ * The same per-match formulas evaluated in exact 128-bit arithmetic, with
+ * general cores summing the exact number of fringe placements; values that
+ * reach 2^128 - 1 saturate (FSGC_FLAG_SATURATED, all words set).  The divisor
+ * is the pattern counted in itself with exact placements.  Ordinary (not
+ * packed) graphs only. */
+#define FSGC_FLAG_SATURATED 0x2u /* the exact total needs more than 128 bits */
+typedef struct fsgc_exact_result {
+  uint64_t count_lo, count_hi; /* exact count = raw / automorphisms */
+  uint64_t raw_lo, raw_hi;     /* exact total of the per-match formulas */
+  uint64_t automorphisms;
+  uint32_t flags;              /* FSGC_FLAG_PATTERN_TOO_LARGE, FSGC_FLAG_SATURATED */
+  int32_t core_type;
+  double device_ms;
+} fsgc_exact_result;
+int fsgc_count_exact(fsgc_ctx* ctx, int gid, const fsgc_matching_order* mo, fsgc_exact_result* out);
+
 /* Many (graph, pattern) tasks in one call; results in task order. */
 typedef struct fsgc_task {
   int32_t gid;

@@ -23,6 +23,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 #include <omp.h>
 
@@ -60,6 +61,59 @@ static inline u64 nck(int n, int k) {
   return r;
 }
 
+// Exact counting: a 128-bit value with a saturation flag (the true value is
+// 2^128 - 1 or more).  Zero times anything is zero.  The binomial is computed
+// in 128 bits from the multiplicative formula, with every intermediate checked.
+struct Xo {
+  u128 v = 0;
+  bool sat = false;
+  Xo() {}
+  Xo(u64 x) : v(x) {}
+  static Xo saturated() { Xo r; r.sat = true; return r; }
+};
+static const u128 kU128Max = ~(u128)0;
+static inline Xo operator+(Xo a, Xo b) {
+  if (a.sat || b.sat) return Xo::saturated();
+  Xo r;
+  r.v = a.v + b.v;
+  if (r.v < a.v || r.v == kU128Max) return Xo::saturated();
+  return r;
+}
+static inline Xo operator*(Xo a, Xo b) {
+  if ((!a.sat && a.v == 0) || (!b.sat && b.v == 0)) return Xo();
+  if (a.sat || b.sat || a.v > (kU128Max - 1) / b.v) return Xo::saturated();
+  Xo r;
+  r.v = a.v * b.v;
+  if (r.v == kU128Max) return Xo::saturated();
+  return r;
+}
+static inline Xo& operator+=(Xo& a, Xo b) { return a = a + b; }
+#pragma omp declare reduction(+ : Xo : omp_out = omp_out + omp_in) initializer(omp_priv = Xo())
+
+static inline Xo nck_exact(int n, int k) {
+  if (k < 0 || n < k) return Xo();
+  k = std::min(k, n - k);
+  u128 r = 1;
+  for (int i = 1; i <= k; i++) {
+    // r = C(n, i-1); C(n, i) = r * (n+1-i) / i, exact
+    const u128 f = (u128)(n + 1 - i);
+    const u128 q = r / (u128)i, m = r % (u128)i;
+    if (q > (kU128Max - 1) / f) return Xo::saturated();
+    const u128 hi = q * f, lo = m * f / (u128)i;
+    if (hi > kU128Max - 1 - lo) return Xo::saturated();
+    r = hi + lo;
+  }
+  Xo x;
+  x.v = r;
+  return x;
+}
+
+template <class T> static inline T nck_t(int n, int k);
+template <> inline u64 nck_t<u64>(int n, int k) { return nck(n, k); }
+template <> inline Xo nck_t<Xo>(int n, int k) { return nck_exact(n, k); }
+static inline bool is_zero(u64 x) { return x == 0; }
+static inline bool is_zero(const Xo& x) { return !x.sat && x.v == 0; }
+
 static inline bool has(const Graph& g, int v, int x) {  // x in N(v)
   return std::binary_search(g.beg(v), g.end(v), x);
 }
@@ -80,47 +134,48 @@ static int common2(const Graph& g, int a, int b) {  // |N(a) & N(b)| by merge
 // Venn regions of a 3-vertex core (src/fringeCount.cu:233-327).  The loop nest
 // below visits the same (i,j,k,a,b,c,d) tuples and forms each term from the same
 // nCk factors as the reference; terms the reference skips with `break` are zero.
-static u64 fc3(const int fr[8], const int venn[8]) {
+template <class T>
+static T fc3(const int fr[8], const int venn[8]) {
   const int fuvw = fr[IUVW], fuv = fr[IUV], fuw = fr[IUW], fvw = fr[IVW];
   const int fu = fr[IU], fv = fr[IV], fw = fr[IW];
   int x_uvw = venn[IUVW], x_uv = venn[IUV], x_uw = venn[IUW], x_vw = venn[IVW];
   const int x_u = venn[IU], x_v = venn[IV], x_w = venn[IW];
   if (x_uvw < fuvw) return 0;
-  const u64 base = nck(x_uvw, fuvw);
+  const T base = nck_t<T>(x_uvw, fuvw);
   x_uvw -= fuvw;
-  u64 total = 0;
+  T total = 0;
   // i of the uv-fringes go into the shared uvw region, the rest into uv
   for (int i = std::min(x_uvw, fuv); i >= 0; i--) {
     if (x_uv < fuv - i) break;
-    const u64 t1 = base * nck(x_uvw, i) * nck(x_uv, fuv - i);
+    const T t1 = base * nck_t<T>(x_uvw, i) * nck_t<T>(x_uv, fuv - i);
     const int r_uvw1 = x_uvw - i, r_uv = x_uv - (fuv - i);
     for (int j = std::min(r_uvw1, fuw); j >= 0; j--) {
       if (x_uw < fuw - j) break;
-      const u64 t2 = t1 * nck(r_uvw1, j) * nck(x_uw, fuw - j);
+      const T t2 = t1 * nck_t<T>(r_uvw1, j) * nck_t<T>(x_uw, fuw - j);
       const int r_uvw2 = r_uvw1 - j, r_uw = x_uw - (fuw - j);
       for (int k = std::min(r_uvw2, fvw); k >= 0; k--) {
         if (x_vw < fvw - k) break;
-        const u64 t3 = t2 * nck(r_uvw2, k) * nck(x_vw, fvw - k);
+        const T t3 = t2 * nck_t<T>(r_uvw2, k) * nck_t<T>(x_vw, fvw - k);
         const int r_uvw3 = r_uvw2 - k, r_vw = x_vw - (fvw - k);
         // u-fringes: a from uvw, b from uv, c from uw, rest from u
         for (int a = std::min(r_uvw3, fu); a >= 0; a--) {
-          const u64 ta = t3 * nck(r_uvw3, a);
+          const T ta = t3 * nck_t<T>(r_uvw3, a);
           const int r_uvw4 = r_uvw3 - a;
           const int pool_v = r_uvw4 + r_vw;  // regions still open to v (uvw + vw)
           for (int b = std::min(r_uv, fu - a); b >= 0; b--) {
-            const u64 tb = ta * nck(r_uv, b);
+            const T tb = ta * nck_t<T>(r_uv, b);
             const int r_uv2 = r_uv - b;
             for (int c = std::min(r_uw, fu - a - b); c >= 0; c--) {
               if (x_u < fu - a - b - c) break;
-              const u64 tc = tb * nck(r_uw, c) * nck(x_u, fu - a - b - c);
+              const T tc = tb * nck_t<T>(r_uw, c) * nck_t<T>(x_u, fu - a - b - c);
               const int r_uw2 = r_uw - c;
               // v-fringes: d from (uvw + vw), rest from (uv + v)
               for (int d = std::min(pool_v, fv); d >= 0; d--) {
                 if (r_uv2 + x_v < fv - d) break;
-                const u64 td = tc * nck(pool_v, d) * nck(r_uv2 + x_v, fv - d);
+                const T td = tc * nck_t<T>(pool_v, d) * nck_t<T>(r_uv2 + x_v, fv - d);
                 // w-fringes: everything still open to w
                 const int pool_w = (pool_v - d) + r_uw2 + x_w;
-                if (pool_w >= fw) total += td * nck(pool_w, fw);
+                if (pool_w >= fw) total += td * nck_t<T>(pool_w, fw);
               }
             }
           }
@@ -190,14 +245,15 @@ struct Sample {
 
 // ---------------------------------------------------------------- vertex core
 // src/fringeCount.cu:2152-2191
-static u64 vertex_core(const MO& mo, const Graph& g, const Sample& s) {
-  if (mo.anchorsets == 0) return (u64)g.n;
-  if (mo.fcnt[0] == 1) return (u64)(g.m / 2);
+template <class T>
+static T vertex_core(const MO& mo, const Graph& g, const Sample& s) {
+  if (mo.anchorsets == 0) return (T)g.n;
+  if (mo.fcnt[0] == 1) return (T)(g.m / 2);
   const int t = mo.fcnt[0];
-  u64 tot = 0;
+  T tot = 0;
 #pragma omp parallel for reduction(+ : tot) schedule(dynamic, 4096)
   for (int v = 0; v < g.n; v++)
-    if (s.take(v) && g.deg(v) >= t) tot += nck(g.deg(v), t);
+    if (s.take(v) && g.deg(v) >= t) tot += nck_t<T>(g.deg(v), t);
   return tot;
 }
 
@@ -205,53 +261,55 @@ static u64 vertex_core(const MO& mo, const Graph& g, const Sample& s) {
 // Worklist: undirected edges (u,v) with v < u by vertex id, pruned by degree
 // (init_wl_edge, src/fringeCount.cu:2054-2103); kernels triangle /
 // tailed_triangle / general_edge_core (1864-2051); dispatch edgeCore 2106-2144.
-static u64 edge_formula(int du, int dv, int c_uv, int f_u, int f_uv, int f_v) {
+template <class T>
+static T edge_formula(int du, int dv, int c_uv, int f_u, int f_uv, int f_v) {
   const int a_uv = c_uv - f_uv;
   if (a_uv < 0) return 0;
   const int c_u = du - 1 - c_uv, c_v = dv - 1 - c_uv;
   const int bound = std::min(f_u, a_uv);
-  u64 acc = 0;
+  T acc = 0;
   for (int j = 0; j <= bound; j++) {
     const int k = f_u - j;
-    u64 term = nck(c_u, k) * nck(a_uv + c_v - j, f_v);
-    if (f_u != f_v) term += nck(c_v, k) * nck(a_uv + c_u - j, f_v);
-    acc += term * nck(a_uv, j);
+    T term = nck_t<T>(c_u, k) * nck_t<T>(a_uv + c_v - j, f_v);
+    if (f_u != f_v) term += nck_t<T>(c_v, k) * nck_t<T>(a_uv + c_u - j, f_v);
+    acc += term * nck_t<T>(a_uv, j);
   }
-  return acc * nck(c_uv, f_uv);
+  return acc * nck_t<T>(c_uv, f_uv);
 }
 
-static u64 edge_core(const MO& mo, const Graph& g, const Sample& s) {
+template <class T>
+static T edge_core(const MO& mo, const Graph& g, const Sample& s) {
   int f[4] = {0, 0, 0, 0};
   for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 3] = mo.fcnt[i];
   const int f_u = std::min(f[1], f[2]), f_uv = f[3], f_v = std::max(f[1], f[2]);
   const bool special = (f_uv == 1) && (f_u == 0 || f_v == 0);
   const int lim1 = special ? 1 : f_u + f_uv;
   const int lim2 = special ? 1 : f_u + f_uv + f_v;
-  u64 tot = 0;
+  T tot = 0;
 #pragma omp parallel for reduction(+ : tot) schedule(dynamic, 64)
   for (int u = 0; u < g.n; u++) {
     const int du = g.deg(u);
     if (du <= lim1) continue;
-    const u64 cu = special ? nck(du - 2, f_v) : 0;
+    const T cu = special ? nck_t<T>(du - 2, f_v) : 0;
     for (const int* p = g.beg(u); p < g.end(u) && *p < u; p++) {
       const int v = *p, dv = g.deg(v);
       if (!(dv > lim1 && du + dv > lim2)) continue;
       if (!s.take(u, v)) continue;
       if (special) {
         // triangles w < v < u
-        const u64 c12 = cu + nck(dv - 2, f_v);
+        const T c12 = cu + nck_t<T>(dv - 2, f_v);
         const int *a = g.beg(u), *ae = g.end(u), *b = g.beg(v), *be = g.end(v);
         while (a < ae && b < be && *a < v && *b < v) {
           if (*a < *b) a++;
           else if (*b < *a) b++;
           else {
             if (f_u == 0 && f_v == 0) tot += 1;
-            else tot += c12 + nck(g.deg(*a) - 2, f_v);
+            else tot += c12 + nck_t<T>(g.deg(*a) - 2, f_v);
             a++; b++;
           }
         }
       } else {
-        tot += edge_formula(du, dv, common2(g, u, v), f_u, f_uv, f_v);
+        tot += edge_formula<T>(du, dv, common2(g, u, v), f_u, f_uv, f_v);
       }
     }
   }
@@ -260,21 +318,22 @@ static u64 edge_core(const MO& mo, const Graph& g, const Sample& s) {
 
 // ---------------------------------------------------------------- wedge core
 // src/fringeCount.cu:1381-1825.
-static u64 wedge_formula(int du, int dv, bool adj, int f_u, int f_uv, int f_v, int c_uv) {
+template <class T>
+static T wedge_formula(int du, int dv, bool adj, int f_u, int f_uv, int f_v, int c_uv) {
   // wedge(): endpoints "u","v" of a wedge whose centre is not counted in c_uv
   const int a_uv = c_uv - f_uv;
   if (a_uv < 0) return 0;
   const int corr = adj ? 2 : 1;
   const int a_u = du - (corr + c_uv), a_v = dv - (corr + c_uv);
   const int bound = std::min(f_u, a_uv);
-  u64 sum = 0;
+  T sum = 0;
   for (int j = 0; j <= bound; j++) {
     const int k = f_u - j;
-    u64 term = nck(a_u, k) * nck(a_uv + a_v - j, f_v);
-    if (f_u != f_v) term += nck(a_v, k) * nck(a_uv + a_u - j, f_v);
-    sum += term * nck(a_uv, j);
+    T term = nck_t<T>(a_u, k) * nck_t<T>(a_uv + a_v - j, f_v);
+    if (f_u != f_v) term += nck_t<T>(a_v, k) * nck_t<T>(a_uv + a_u - j, f_v);
+    sum += term * nck_t<T>(a_uv, j);
   }
-  return sum * nck(c_uv, f_uv);
+  return sum * nck_t<T>(c_uv, f_uv);
 }
 
 // Exclusive Venn sizes of N(u),N(v),N(w) for a wedge or triangle centred at u,
@@ -293,7 +352,8 @@ static void venn3_wedge(const Graph& g, int u, int v, int w, int p12, int venn[8
   venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
 }
 
-static u64 wedge_core(const MO& mo, const Graph& g, const Sample& s) {
+template <class T>
+static T wedge_core(const MO& mo, const Graph& g, const Sample& s) {
   int f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 7] = mo.fcnt[i];
   if (mo.list[1] == 2) {  // centre is B: swap roles of A and B
@@ -307,7 +367,7 @@ static u64 wedge_core(const MO& mo, const Graph& g, const Sample& s) {
   const int sum2 = sum3 - std::max(std::max(min_u, min_v), min_w);
   const int sum1 = std::min(std::min(min_u, min_v), min_w);
   const int lim = std::min(min_v, min_w);
-  u64 tot = 0;
+  T tot = 0;
   if (f[IUVW] == 0 && f[IUV] == 0 && f[IUW] == 0 && f[IU] == 0) {
     // centre has no fringes: init_wl_specialized_wedge + wedgecore_specialized
     const int fv = f[IV], fvw = f[IVW], fw = f[IW];
@@ -322,7 +382,7 @@ static u64 wedge_core(const MO& mo, const Graph& g, const Sample& s) {
           const int w = *pw, dw = g.deg(w);
           if (dw < thres) continue;
           const int c = common2(g, v, w) - 1;
-          tot += wedge_formula(dv, dw, has(g, w, v), fv, fvw, fw, c);
+          tot += wedge_formula<T>(dv, dw, has(g, w, v), fv, fvw, fw, c);
         }
       }
     }
@@ -351,13 +411,13 @@ static u64 wedge_core(const MO& mo, const Graph& g, const Sample& s) {
           if (!(u < w)) continue;
           venn3_wedge(g, u, v, w, p12, venn);
           venn[IUV]--; venn[IUW]--; venn[IVW]--;
-          for (int r = 0; r < rot; r++) tot += fc3(fr[r], venn);
+          for (int r = 0; r < rot; r++) tot += fc3<T>(fr[r], venn);
         } else {
           if (!(cond && dw >= thres1)) continue;
           venn3_wedge(g, u, v, w, p12, venn);
           venn[IU] -= 2; venn[IVW]--;
-          tot += fc3(fr[0], venn);
-          if (rot > 3) tot += fc3(fr[3], venn);
+          tot += fc3<T>(fr[0], venn);
+          if (rot > 3) tot += fc3<T>(fr[3], venn);
         }
       }
     }
@@ -388,7 +448,8 @@ static bool triangle_relabel_gate(const Graph& g) {
   return maxd > 16;
 }
 
-static u64 triangle_core(const MO& mo, const Graph& g, const Sample& s) {
+template <class T>
+static T triangle_core(const MO& mo, const Graph& g, const Sample& s) {
   int f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 7] = mo.fcnt[i];
   const int min_u = f[IUVW] + f[IUV] + f[IUW] + f[IU];
@@ -403,7 +464,7 @@ static u64 triangle_core(const MO& mo, const Graph& g, const Sample& s) {
   const bool clique = (f[IUVW] == 1) && (f[IUV] + f[IUW] + f[IVW] == 0) &&
                       ((f[IU] == 0) + (f[IV] == 0) + (f[IW] == 0) >= 2);
   const int tails = f[IU] + f[IV] + f[IW];
-  u64 tot = 0;
+  T tot = 0;
 #pragma omp parallel for reduction(+ : tot) schedule(dynamic, 16)
   for (int u = 0; u < g.n; u++) {
     const int du = g.deg(u);
@@ -420,16 +481,16 @@ static u64 triangle_core(const MO& mo, const Graph& g, const Sample& s) {
       for (const int* pw = g.beg(u); pw < g.end(u); pw++)
         if (ord.key(*pw) < kv && has(g, v, *pw)) ws.push_back(*pw);
       if (clique) {
-        const u64 c12 = nck(du - 3, tails) + nck(dv - 3, tails);
+        const T c12 = nck_t<T>(du - 3, tails) + nck_t<T>(dv - 3, tails);
         for (int w : ws) {
           const int dw = g.deg(w);
           if (dw < 3) continue;
           const long long kw = ord.key(w);
-          const u64 c123 = c12 + nck(dw - 3, tails);
+          const T c123 = c12 + nck_t<T>(dw - 3, tails);
           for (const int* pq = g.beg(w); pq < g.end(w); pq++) {
             const int q = *pq;
             if (ord.key(q) < kw && has(g, u, q) && has(g, v, q))
-              tot += (tails == 0) ? 1 : c123 + nck(g.deg(q) - 3, tails);
+              tot += (tails == 0) ? 1 : c123 + nck_t<T>(g.deg(q) - 3, tails);
           }
         }
         continue;
@@ -451,7 +512,7 @@ static u64 triangle_core(const MO& mo, const Graph& g, const Sample& s) {
         venn[IV] = dv - (c12 + c23 + (c123 + 2));
         venn[IW] = dw - (c13 + c23 + (c123 + 2));
         venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
-        for (int r = 0; r < rot; r++) tot += fc3(fr[r], venn);
+        for (int r = 0; r < rot; r++) tot += fc3<T>(fr[r], venn);
       }
     }
   }
@@ -515,30 +576,33 @@ static void venn_general(GenCtx& c) {
 // set, visited in increasing bitmap order, with the remainder going to the
 // region of all anchors.  Each placement contributes the product of
 // nCk(remaining region size, fringes put there).
-static u64 place(GenCtx& c, int asi, int idx, int remaining);
-static u64 place_set(GenCtx& c, int asi) {
+template <class T>
+static T place(GenCtx& c, int asi, int idx, int remaining);
+template <class T>
+static T place_set(GenCtx& c, int asi) {
   const int anch = c.mo->anch[asi];
-  return place(c, asi, anch, c.mo->fcnt[asi]);
+  return place<T>(c, asi, anch, c.mo->fcnt[asi]);
 }
-static u64 place(GenCtx& c, int asi, int idx, int remaining) {
+template <class T>
+static T place(GenCtx& c, int asi, int idx, int remaining) {
   const int top = c.anchors;
   const int anch = c.mo->anch[asi];
   if (idx == top) {
-    const u64 w = nck(c.venn[top], remaining);
-    if (w == 0) return 0;
+    const T w = nck_t<T>(c.venn[top], remaining);
+    if (is_zero(w)) return T(0);
     if (asi == 0) return w;
     c.venn[top] -= remaining;
-    const u64 r = w * place_set(c, asi - 1);
+    const T r = w * place_set<T>(c, asi - 1);
     c.venn[top] += remaining;
     return r;
   }
   const int next = (((idx | c.nonanchors) + 1) | anch) & ~c.nonanchors;
-  u64 s = 0;
+  T s = T(0);
   for (int a = std::min(c.venn[idx], remaining); a >= 0; a--) {
-    const u64 w = nck(c.venn[idx], a);
-    if (w == 0) continue;
+    const T w = nck_t<T>(c.venn[idx], a);
+    if (is_zero(w)) continue;
     c.venn[idx] -= a;
-    s += w * place(c, asi, next, remaining - a);
+    s += w * place<T>(c, asi, next, remaining - a);
     c.venn[idx] += a;
   }
   return s;
@@ -600,14 +664,16 @@ static u64 place_reference(GenCtx& c, int* fr) {
 
 static int g_exact_placements = 0;  // 1: exact placement sum, 0: the reference's functionX
 
-static u64 gen_dfs(GenCtx& c, int level) {
+// T = Xo (exact counts) always sums the exact placements.
+template <class T>
+static T gen_dfs(GenCtx& c, int level) {
   // choose stack[level+1]
   const MO& mo = *c.mo;
   const Graph& g = *c.g;
   const int list = mo.list[level];
   const int first = __builtin_ctz(list);
   const int src = c.stack[first];
-  u64 sum = 0;
+  T sum = T(0);
   for (const int* p = g.beg(src); p < g.end(src); p++) {
     const int x = *p;
     if (g.deg(x) < mo.destdeg[level]) continue;
@@ -623,25 +689,26 @@ static u64 gen_dfs(GenCtx& c, int level) {
     c.stack[level + 1] = x;
     if (level + 1 == c.k - 1) {
       venn_general(c);
-      if (g_exact_placements) {
-        sum += place_set(c, mo.anchorsets - 1);
+      if (g_exact_placements || !std::is_same<T, u64>::value) {
+        sum += place_set<T>(c, mo.anchorsets - 1);
       } else {
         int fr[64] = {0};
         for (int i = 0; i < mo.anchorsets; i++) fr[mo.anch[i]] = mo.fcnt[i];
         sum += place_reference(c, fr);
       }
     } else {
-      sum += gen_dfs(c, level + 1);
+      sum += gen_dfs<T>(c, level + 1);
     }
   }
   return sum;
 }
 
-static u64 general_core(const MO& mo, const Graph& g, const Sample& s) {
+template <class T>
+static T general_core(const MO& mo, const Graph& g, const Sample& s) {
   int anchors = 0;
   for (int i = 0; i < mo.anchorsets; i++) anchors |= mo.anch[i];
   const int k = mo.nodes;
-  u64 tot = 0;
+  T tot = T(0);
 #pragma omp parallel for reduction(+ : tot) schedule(dynamic, 4)
   for (int u = 0; u < g.n; u++) {
     if (g.deg(u) < mo.startdeg) continue;
@@ -653,7 +720,7 @@ static u64 general_core(const MO& mo, const Graph& g, const Sample& s) {
       if (g.deg(v) < mo.destdeg[0] || !s.take(u, v)) continue;  // init_wl_general
       c.stack[0] = u;
       c.stack[1] = v;
-      tot += gen_dfs(c, 1);
+      tot += gen_dfs<T>(c, 1);
     }
   }
   return tot;
@@ -684,16 +751,17 @@ static void pattern_graph(const MO& mo, std::vector<long long>& idx, std::vector
   }
 }
 
-static u64 count_core(const MO& mo, const Graph& g, const Sample& s, int* core_type) {
-  if (mo.nodes == 1) { *core_type = 1; return vertex_core(mo, g, s); }
-  if (mo.nodes == 2) { *core_type = 2; return edge_core(mo, g, s); }
+template <class T>
+static T count_core(const MO& mo, const Graph& g, const Sample& s, int* core_type) {
+  if (mo.nodes == 1) { *core_type = 1; return vertex_core<T>(mo, g, s); }
+  if (mo.nodes == 2) { *core_type = 2; return edge_core<T>(mo, g, s); }
   if (mo.nodes == 3) {
-    if (__builtin_popcount(mo.list[1]) == 1) { *core_type = 3; return wedge_core(mo, g, s); }
+    if (__builtin_popcount(mo.list[1]) == 1) { *core_type = 3; return wedge_core<T>(mo, g, s); }
     *core_type = 4;
-    return triangle_core(mo, g, s);
+    return triangle_core<T>(mo, g, s);
   }
   *core_type = 5;
-  return general_core(mo, g, s);
+  return general_core<T>(mo, g, s);
 }
 
 }  // namespace
@@ -730,17 +798,66 @@ int oracle_count(int n, const long long* idx, const int* adj, const unsigned cha
       return 0;
     }
     Graph pg{pn, pidx[pn], pidx.data(), padj.data()};
-    aut = count_core(mo, pg, Sample(), &ct);
+    aut = count_core<u64>(mo, pg, Sample(), &ct);
     // the reference divides by an int (src/fringeCount.cu:2213, 2230)
     aut = (u64)(unsigned int)(int)aut;
     if (aut == 0) return -2;
   }
-  const u64 raw = count_core(mo, g, s, &ct);
+  const u64 raw = count_core<u64>(mo, g, s, &ct);
   out[0] = raw / aut;
   out[1] = raw;
   out[2] = aut;
   out[3] = (u64)ct;
   return 0;
+}
+
+// Exact count (128-bit, saturating) of the same pattern: the same per-match
+// formulas in exact arithmetic, general cores with the exact placement sum.
+// out[0..1] count (lo, hi) = raw / divisor, out[2..3] raw total, out[4] divisor
+// (exact placements, as the divisor of the exact count), out[5] core type,
+// out[6] flags: 1 = pattern larger than the graph (count 0), 2 = saturated.
+int oracle_count_exact(int n, const long long* idx, const int* adj, const unsigned char* mo_bytes, int threads,
+                       unsigned long long* out) {
+  MO mo;
+  memcpy(&mo, mo_bytes, sizeof(MO));
+  if (mo.nodes < 1 || mo.nodes > 6 || mo.anchorsets > 63) return -1;
+  if (threads > 0) omp_set_num_threads(threads);
+  Graph g{n, idx[n], idx, adj};
+  for (int i = 0; i < 7; i++) out[i] = 0;
+  u64 aut = 1;
+  int ct = 0;
+  if (mo.nodes >= 3) {
+    std::vector<long long> pidx;
+    std::vector<int> padj;
+    pattern_graph(mo, pidx, padj);
+    const int pn = (int)pidx.size() - 1;
+    if (pn > n || pidx[pn] > g.m) {
+      out[5] = (mo.nodes == 3) ? ((__builtin_popcount(mo.list[1]) == 1) ? 3 : 4) : 5;
+      out[6] = 1;
+      return 0;
+    }
+    Graph pg{pn, pidx[pn], pidx.data(), padj.data()};
+    const Xo a = count_core<Xo>(mo, pg, Sample(), &ct);
+    if (a.sat || a.v == 0 || a.v > 0xffffffffULL) return -2;
+    aut = (u64)a.v;
+  }
+  const Xo raw = count_core<Xo>(mo, g, Sample(), &ct);
+  out[5] = (u64)ct;
+  out[4] = aut;
+  if (raw.sat) {
+    out[6] = 2;
+    return 0;
+  }
+  const u128 q = raw.v / aut;
+  out[0] = (u64)q; out[1] = (u64)(q >> 64);
+  out[2] = (u64)raw.v; out[3] = (u64)(raw.v >> 64);
+  return 0;
+}
+
+// Exact binomial, for unit tests: out[0..1] = C(n, k) (lo, hi), out[2] = saturated.
+void oracle_nck_exact(int n, int k, unsigned long long* out) {
+  const Xo x = nck_exact(n, k);
+  out[0] = (u64)x.v; out[1] = (u64)(x.v >> 64); out[2] = x.sat ? 1 : 0;
 }
 
 // General-core placement sums: 0 (default) follows the reference's functionX
@@ -749,7 +866,7 @@ void oracle_set_exact_placements(int on) { g_exact_placements = on ? 1 : 0; }
 
 // Per-call building blocks exposed for unit tests.
 unsigned long long oracle_nck(int n, int k) { return nck(n, k); }
-unsigned long long oracle_fc3(const int* fr8, const int* venn8) { return fc3(fr8, venn8); }
+unsigned long long oracle_fc3(const int* fr8, const int* venn8) { return fc3<u64>(fr8, venn8); }
 int oracle_rotations(const int* f8, int wedge, int* fr48) {
   int fr[6][8];
   const int p = rotations3(f8, fr, wedge != 0);

@@ -40,6 +40,11 @@ def lib():
         L.oracle_fc3.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.oracle_rotations.restype = C.c_int
         L.oracle_rotations.argtypes = [C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int)]
+        L.oracle_count_exact.restype = C.c_int
+        L.oracle_count_exact.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int,
+                                         C.POINTER(C.c_ulonglong)]
+        L.oracle_nck_exact.restype = None
+        L.oracle_nck_exact.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_ulonglong)]
         L.oracle_bruteforce.restype = C.c_int
         L.oracle_bruteforce.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int,
                                         C.POINTER(C.c_ulonglong)]
@@ -63,6 +68,28 @@ def count(nindex, nlist, mo_bytes, stride=1, phase=0, threads=0, exact_placement
     if st != 0:
         raise RuntimeError(f"oracle_count failed ({st})")
     return {"count": out[0], "raw": out[1], "aut": out[2], "core": out[3]}
+
+
+def count_exact(nindex, nlist, mo_bytes, threads=0):
+    """Exact count in 128 bits: dict(count, raw, aut, core, too_large, saturated);
+    the same per-match formulas in exact arithmetic, exact fringe placements."""
+    idx = np.ascontiguousarray(nindex, dtype=np.int64)
+    adj = np.ascontiguousarray(nlist, dtype=np.int32)
+    if len(adj) == 0:
+        adj = np.zeros(1, np.int32)
+    out = (C.c_ulonglong * 7)()
+    st = lib().oracle_count_exact(len(idx) - 1, idx.ctypes.data, adj.ctypes.data, bytes(mo_bytes), threads, out)
+    if st != 0:
+        raise RuntimeError(f"oracle_count_exact failed ({st})")
+    return {"count": out[0] | (out[1] << 64), "raw": out[2] | (out[3] << 64), "aut": out[4], "core": out[5],
+            "too_large": bool(out[6] & 1), "saturated": bool(out[6] & 2)}
+
+
+def nck_exact(n, k):
+    """Exact binomial in 128 bits: (value, saturated)."""
+    out = (C.c_ulonglong * 3)()
+    lib().oracle_nck_exact(n, k, out)
+    return out[0] | (out[1] << 64), bool(out[2])
 
 
 def bruteforce(nindex, nlist, n_pattern, edges):

@@ -101,3 +101,4 @@ def test_struct_layouts_match_the_header():
     assert C.sizeof(fsgc.Task) == 144
     assert C.sizeof(fsgc.Result) == 40
     assert C.sizeof(fsgc.ServerStats) == 56
+    assert C.sizeof(fsgc.ExactResult) == 56
