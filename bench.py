@@ -299,11 +299,24 @@ def run_gpu(args, rank, world):
     barrier()
     for a, b in zip(res_h, ref_res):
         assert a.count == b.count
+    # exact 128-bit counts beside the reference-compatible u64 ones (untimed)
+    exact = {}
+    if args.exact:
+        gid = ctx.upload(g)
+        try:
+            for (name, mo), r in zip(mos, ref_res):
+                x = ctx.count_exact(gid, mo)
+                exact[name] = {"exact": "saturated" if x.saturated else str(x.count),
+                               "u64_wrapped": x.saturated or x.raw_total != r.raw_total}
+        except fsgc.FsgcError as e:  # reported, not fatal: the timed numbers stand
+            exact["error"] = str(e)
+        ctx.release(gid)
     t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], world)
     out = {
         "per_task_ms": {name: per_task[i] / args.steps for i, (name, _) in enumerate(mos)},
         "prep_ms": statistics.mean(prep_ms),
         "counts": {name: int(r.count) for (name, _), r in zip(mos, ref_res)},
+        "exact": exact,
         "cores": {name: int(r.core_type) for (name, _), r in zip(mos, ref_res)},
         "t_dev": t_dev, "t_e2e": t_e2e, "launches": launches, "clocks": clk.summary(), "gen_s": gen_s,
         "graph": {"n": g.n, "m": g.m, "max_degree": int(g.degrees().max())},
@@ -494,6 +507,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
     ap.add_argument("--scale", type=int, default=None, help="RMAT scale (profiling runs; default 22)")
     ap.add_argument("--patterns", default=None, help="comma-separated subset of the patterns (profiling runs)")
+    ap.add_argument("--no-exact", dest="exact", action="store_false",
+                    help="skip the untimed exact 128-bit counts reported beside the u64 ones")
     args = ap.parse_args()
     if args.patterns:
         args.patterns = args.patterns.split(",")
@@ -574,7 +589,7 @@ def main():
                    "l2": "inputs (0.5 GB CSR) larger than L2, and L2 flushed before every timed step",
                    "prep_ms": round(out["prep_ms"], 3),
                    "per_pattern_ms": {k: round(v, 3) for k, v in out["per_task_ms"].items()},
-                   "counts": out["counts"]},
+                   "counts": out["counts"], "exact_counts": out["exact"]},
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * len(mos)},
