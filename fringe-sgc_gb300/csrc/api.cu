@@ -906,6 +906,18 @@ unsigned long long fsgc_nck_host(int n, int k) {
   return fsgc::nck_ref(n, k, tab);
 }
 
+// Host evaluation of the exact 128-bit arithmetic of the counting kernels (the
+// same __host__ __device__ code), for tests without a GPU: op 0 = a + b,
+// 1 = a * b, 2 = C(n, k).  out = (lo, hi, saturated).
+void fsgc_x128_host(int op, unsigned long long a_lo, unsigned long long a_hi, unsigned long long b_lo,
+                    unsigned long long b_hi, int n, int k, unsigned long long* out) {
+  const fsgc::X128 a(a_lo, a_hi), b(b_lo, b_hi);
+  const fsgc::X128 r = (op == 0) ? a + b : (op == 1) ? a * b : fsgc::nck_x(n, k);
+  out[0] = r.lo;
+  out[1] = r.hi;
+  out[2] = r.is_saturated() ? 1 : 0;
+}
+
 unsigned long long fsgc_div_small_host(unsigned long long x, unsigned d) {
   if (d < 2 || d >= (unsigned)fsgc::kMaxDiv) return 0;
   return fsgc::div_magic(x, fsgc::make_div_magic(d));
