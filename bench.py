@@ -464,7 +464,7 @@ def run_serve(args):
             d = direct[(gi, pi)]
             assert (r.count, r.raw_total) == (d.count, d.raw_total), (gi, pi)
         return {"queries_per_s": st.queries_per_s, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms,
-                "rounds": int(st.rounds), "wall_s": wall}
+                "rounds": int(st.rounds), "cache_hits": int(st.cache_hits), "wall_s": wall}
 
     launches0 = ctx.launches
     poisson = serve(args.lanes, 64, True)

@@ -13,7 +13,9 @@
 // different batches overlaps on the device and no query waits for a batch
 // that was already running when it arrived.  A batch the checks refuse is
 // re-run one query at a time, so that a bad query fails alone.  Latency is
-// submission to completion.
+// submission to completion.  Results are cached by (graph, matching-order
+// bytes): resident graphs never change and graph ids are never reused, so a
+// repeated query completes at submission without device work.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -21,6 +23,8 @@
 #include <deque>
 #include <map>
 #include <mutex>
+#include <string>
+#include <utility>
 #include <thread>
 #include <vector>
 
@@ -64,6 +68,9 @@ struct fsgc_server {
   std::vector<LaneSlot> lanes;
   std::vector<std::thread> workers;
   std::map<int, int> graphs;  // registered graph ids
+  std::map<std::pair<int, std::string>, fsgc_result> cache;  // completed counts
+  static constexpr size_t kCacheCap = 1 << 16;               // entries; cleared when full
+  uint64_t cache_hits = 0;
   // statistics
   std::vector<double> latencies;
   uint64_t completed = 0, rounds = 0;
@@ -143,6 +150,10 @@ void worker_loop(fsgc_server* s, int li) {
         q.status = status[i];
         q.result = results[i];
         q.done = true;
+        if (q.status == FSGC_OK) {
+          if (s->cache.size() >= fsgc_server::kCacheCap) s->cache.clear();
+          s->cache[{q.gid, std::string(reinterpret_cast<const char*>(&q.mo), sizeof(q.mo))}] = q.result;
+        }
         q.latency_ms = std::chrono::duration<double, std::milli>(now - q.submitted).count();
         s->latencies.push_back(q.latency_ms);
         s->completed++;
@@ -244,6 +255,30 @@ int fsgc_server_submit(fsgc_server* s, int gid, const fsgc_matching_order* mo, u
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->graphs.find(gid) == s->graphs.end()) return FSGC_ENOTFOUND;
+    auto hit = s->cache.find({gid, std::string(reinterpret_cast<const char*>(mo), sizeof(*mo))});
+    if (hit != s->cache.end()) {
+      Query q;
+      q.ticket = s->next_ticket++;
+      q.gid = gid;
+      q.mo = *mo;
+      q.footprint = 0;
+      q.submitted = t0;
+      q.done = true;
+      q.result = hit->second;
+      const auto now = Clock::now();
+      q.latency_ms = std::chrono::duration<double, std::milli>(now - t0).count();
+      if (!s->any) {
+        s->first_submit = t0;
+        s->any = true;
+      }
+      s->latencies.push_back(q.latency_ms);
+      s->completed++;
+      s->cache_hits++;
+      s->last_done = now;
+      s->queries[q.ticket] = q;
+      *ticket = q.ticket;
+      return FSGC_OK;
+    }
   }
   fsgc_task task;
   task.gid = gid;
@@ -309,6 +344,7 @@ int fsgc_server_stats_get(fsgc_server* s, fsgc_server_stats* out) {
   out->rounds = s->rounds;
   out->queued = s->waiting.size();
   out->in_use_bytes = s->held_total;
+  out->cache_hits = s->cache_hits;
   out->p50_ms = percentile(s->latencies, 0.50);
   out->p99_ms = percentile(s->latencies, 0.99);
   if (s->completed > 0 && s->any) {

@@ -75,7 +75,7 @@ class ExactResult(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_uint64), ("rounds", C.c_uint64), ("queued", C.c_uint64),
                 ("in_use_bytes", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
-                ("queries_per_s", C.c_double)]
+                ("queries_per_s", C.c_double), ("cache_hits", C.c_uint64)]
 
 
 class FsgcError(RuntimeError):

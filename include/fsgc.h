@@ -238,7 +238,9 @@ int fsgc_task_footprint(fsgc_ctx* ctx, const fsgc_task* task, size_t* bytes);
  * completes them when they finish, while the other lanes keep admitting and
  * running queries that arrived in the meantime.  A query whose footprint alone
  * exceeds the budget is refused at submission (FSGC_EBUSY); a query that fails
- * fails alone.  Latency is submission to completion. */
+ * fails alone.  Latency is submission to completion.  Completed counts are
+ * cached by (graph, matching-order bytes); a repeated query completes at
+ * submission. */
 typedef struct fsgc_server fsgc_server;
 typedef struct fsgc_server_stats {
   uint64_t completed;    /* queries finished */
@@ -247,6 +249,7 @@ typedef struct fsgc_server_stats {
   uint64_t in_use_bytes; /* work-arena bytes the lanes hold or have reserved */
   double p50_ms, p99_ms; /* latency percentiles over completed queries */
   double queries_per_s;  /* completed / (last completion - first submission) */
+  uint64_t cache_hits;   /* queries answered from the result cache at submission */
 } fsgc_server_stats;
 int fsgc_server_create(fsgc_ctx* ctx, size_t memory_budget, int lanes, int max_batch, fsgc_server** out);
 /* Finishes every submitted query, then stops the worker. */

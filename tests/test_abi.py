@@ -100,5 +100,5 @@ def test_struct_layouts_match_the_header():
     assert C.sizeof(fsgc.MatchingOrder) == 139
     assert C.sizeof(fsgc.Task) == 144
     assert C.sizeof(fsgc.Result) == 40
-    assert C.sizeof(fsgc.ServerStats) == 56
+    assert C.sizeof(fsgc.ServerStats) == 64
     assert C.sizeof(fsgc.ExactResult) == 56

@@ -83,6 +83,12 @@ def test_bad_query_fails_alone_and_admission_refuses(ctx):
                 srv.wait(ts[1])
             r2, _ = srv.wait(ts[2])
             assert r0.count == r2.count == ctx.count(gid, good).count
+            # a repeated query is answered from the result cache at submission
+            hits = srv.stats().cache_hits
+            r3, _ = srv.wait(srv.submit(gid, good))
+            assert r3.count == r0.count and srv.stats().cache_hits == hits + 1
+            with pytest.raises(fsgc.FsgcError):  # failures are not cached
+                srv.wait(srv.submit(gid, bad))
             with pytest.raises(fsgc.FsgcError):
                 srv.submit(gid + 1000, good)  # unregistered graph
         # a hub graph whose wedge count needs a hub-cursor arena
