@@ -128,6 +128,12 @@ void worker_loop(fsgc_server* s, int li) {
             s->cv_work.notify_all();
             continue;
           }
+          // nothing of ours to give back: wake the idle lanes that hold an
+          // arena (each either admits the head with it or gives it back);
+          // lanes that are counting wake everyone when they finish
+          bool others_hold = false;
+          for (const LaneSlot& l : s->lanes) others_hold = others_hold || (&l != &ls && !l.busy && l.held > 0);
+          if (others_hold) s->cv_work.notify_all();
         }
         s->cv_work.wait(lk);
       }
