@@ -69,3 +69,21 @@ def test_exact_closed_forms_where_u64_wraps():
         want = math.comb(L - 2, f) * math.comb(L, f)
         assert (want >= U128_MAX) == saturates
         assert x["saturated"] if saturates else (x["count"] == want and not x["saturated"]), f
+
+
+def test_exact_matches_bruteforce_on_random_and_predefined_patterns():
+    from helpers import golden_cases
+    g = fsgc.gen_er(30, 90, 11)
+    cases = [(f"pre{k}", fsgc.predefined_pattern(k)) for k in range(31)]
+    cases += [(c["name"], (c["n"], [tuple(e) for e in c["edges"]])) for c in golden_cases("random")
+              if c["mo"] is not None and c["n"] <= 8][:40]
+    checked = 0
+    for name, (n, edges) in cases:
+        if n > 8:
+            continue
+        mo = fsgc.preprocess(n, edges).to_bytes()
+        x = oracle.count_exact(g.nindex, g.nlist, mo)
+        b, _ = oracle.bruteforce(g.nindex, g.nlist, n, edges)
+        assert x["count"] == b and not x["saturated"], name
+        checked += 1
+    assert checked >= 30
