@@ -189,7 +189,10 @@ void worker_loop(fsgc_server* s, int li) {
       std::lock_guard<std::mutex> lk(s->mu);
       LaneSlot& ls = s->lanes[(size_t)li];
       s->rounds++;
-      // the arena now held, as allocated
+      // Keep the arena for the next batch only while nothing waits: with
+      // queries queued, an idle lane holding budget would keep the other lanes
+      // from admitting them (the arena is stream-ordered, so regrowing it is cheap).
+      if (!s->waiting.empty()) fsgc_lane_trim(lane);
       const size_t real = fsgc_lane_scratch_bytes(lane);
       s->held_total = s->held_total - ls.held + real;
       ls.held = real;
