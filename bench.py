@@ -16,6 +16,18 @@ each result read back to the host.
           Arm host), on a bounded sample of each pattern's work items,
           extrapolated to the whole workload
 
+Untimed, after the measurement, the line also carries the exact 128-bit count
+of each pattern (fsgc_count_exact) beside the reference-compatible u64 one, and
+whether the u64 arithmetic wrapped (--no-exact skips it).
+
+Other workloads (one JSON line each, not the default):
+  --workload packed   batching across graphs: seeded Chung-Lu member graphs in
+                      one packed CSR, one count per pattern, against one
+                      fsgc_count per (graph, pattern)
+  --workload serve    the serving loop: resident RMAT graphs, Poisson arrivals
+                      of (graph, pattern) queries, p50/p99 latency, then the
+                      same queries as a burst with and without batching
+
 Multi-GPU: replicas only (each rank counts the whole workload on its own
 GPU); value = all ranks' patterns / the slowest rank's time.
 """
