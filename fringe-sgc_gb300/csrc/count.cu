@@ -752,7 +752,7 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
               eval_pair<BIG, A>(g, p, S, lo, wd, word, g.deg[w], v, dv, thres, acc);
             } else {
               const int o0 = wd << lper;
-              const unsigned cmask = (bits == 16) ? 0xffffu : ((1u << bits) - 1);
+              const unsigned cmask = (1u << (bits & 31)) - 1;  // bits is 4, 8 or 16 here
               for (unsigned rest = word; rest; ) {
                 const int k = (__ffs(rest) - 1) / bits;  // next non-zero counter of the word
                 const unsigned C = (word >> (k * bits)) & cmask;
@@ -1277,7 +1277,7 @@ void triangle_bitmap_geometry(const DevGraph& G, long long* per_block, int* bloc
       1, std::min<size_t>((size_t)sm_count() * 3, budget / (sizeof(unsigned) * (size_t)*per_block)));
 }
 
-bool triangle_uses_bitmaps(const fsgc_matching_order& mo, const DevGraph& G, int mode) {
+bool triangle_uses_bitmaps(const fsgc_matching_order&, const DevGraph& G, int mode) {
   const size_t smem = (size_t)3 * sizeof(int) * (size_t)std::max(1LL, G.max_outdeg);
   return mode == 0 && smem <= (size_t)96 * 1024 && G.m / 2 > 0;
 }
