@@ -207,6 +207,12 @@ def kernel_bytes(name, core, g):
     return None
 
 
+def edges_per_second(m, per_pattern_ms):
+    """The reference harness's throughput figure per pattern: directed CSR
+    entries / count seconds (reproduce.py:91)."""
+    return {k: (m / (ms / 1000.0) if ms > 0 else None) for k, ms in per_pattern_ms.items()}
+
+
 def measured_traffic(pattern, g):
     """DRAM bytes (read + write) of one count of `pattern` on this graph, from the
     ncu capture recorded in profiles/dram_traffic.json (null when the capture
@@ -601,6 +607,8 @@ def main():
                    "l2": "inputs (0.5 GB CSR) larger than L2, and L2 flushed before every timed step",
                    "prep_ms": round(out["prep_ms"], 3),
                    "per_pattern_ms": {k: round(v, 3) for k, v in out["per_task_ms"].items()},
+                   "edges_per_s": {k: (round(v, 1) if v is not None else None)
+                                   for k, v in edges_per_second(g.m, out["per_task_ms"]).items()},
                    "counts": out["counts"], "exact_counts": out["exact"]},
         "roofline": roof,
         "cpu_baseline": cpu,

@@ -1,0 +1,52 @@
+"""bench.py's JSON line, assembled on the CPU from a stand-in of the GPU run
+(the measured values are made up; only the line's keys, units and arithmetic
+are checked): the fields of the benchmark contract, roofline, e2e, CPU baseline,
+edges/s and exact counts."""
+import json
+import os
+import sys
+
+import pytest
+
+import fsgc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402
+
+
+class _Ctx:
+    def close(self):
+        pass
+
+
+def test_default_line_has_the_contract_fields(monkeypatch, capsys):
+    g = fsgc.gen_rmat(10, 8, seed=3)
+    mos = bench.matching_orders()
+    names = [n for n, _ in mos]
+    per = {n: 10.0 + i for i, n in enumerate(names)}
+    out = {"per_task_ms": per, "prep_ms": 1.5, "counts": {n: 7 for n in names},
+           "cores": {n: (3 if "wedge_1_on_each_end" in n else 1) for n in names},
+           "exact": {n: {"exact": "7", "u64_wrapped": False} for n in names},
+           "t_dev": 0.2, "t_e2e": 0.25, "launches": 21, "clocks": {"sm_mhz": 2000.0, "sm_max_mhz": 2070.0,
+                                                                     "reasons": [], "samples": 9},
+           "gen_s": 0.1, "graph": {"n": g.n, "m": g.m, "max_degree": int(g.degrees().max())}}
+    monkeypatch.setattr(bench, "run_gpu", lambda args, rank, world: (out, g, mos, _Ctx()))
+    monkeypatch.setattr(bench, "cpu_sample", lambda g, mos, budget, threads: (100.0, {n: 1 for n in names}))
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--steps", "2", "--warmup", "3"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "roofline", "cpu_baseline", "e2e",
+                "gpu_launches", "clocks"):
+        assert key in line, key
+    assert line["value"] == pytest.approx(len(mos) * 2 / 0.2)
+    assert line["e2e"]["value"] == pytest.approx(len(mos) * 2 / 0.25)
+    assert line["e2e"]["h2d_bytes_per_step"] == 8 * (g.n + 1) + 4 * g.m
+    r = line["roofline"]
+    assert r["kernel"] == max(per, key=per.get) and r["unit"] == "GB/s" and r["peak"] > 0
+    assert r["frac"] == pytest.approx(r["achieved"] / r["peak"], rel=1e-3)
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == pytest.approx(len(mos) / 100.0)
+    c = line["config"]
+    assert c["workload"].startswith("RMAT") and set(c["edges_per_s"]) == set(names)
+    assert c["exact_counts"][names[0]]["exact"] == "7"

@@ -93,3 +93,10 @@ def test_traffic_record_only_for_its_own_workload():
     assert bench.measured_traffic("4cycle_opposite", G) is None
     G.n = 1048576
     assert bench.measured_traffic("wedge_1_on_each_end", G) is None
+
+
+def test_edges_per_second_is_entries_over_seconds():
+    sys.path.insert(0, ROOT)
+    import bench
+    e = bench.edges_per_second(128312556, {"a": 1000.0, "b": 0.0, "c": 250.0})
+    assert e == {"a": 128312556.0, "b": None, "c": 513250224.0}
