@@ -50,3 +50,17 @@ def test_default_line_has_the_contract_fields(monkeypatch, capsys):
     c = line["config"]
     assert c["workload"].startswith("RMAT") and set(c["edges_per_s"]) == set(names)
     assert c["exact_counts"][names[0]]["exact"] == "7"
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    g = fsgc.gen_rmat(8, 4, seed=1)
+    monkeypatch.setattr(bench, "workload_graph", lambda scale=None: (g, 0.0))
+    monkeypatch.setattr(bench, "cpu_sample", lambda g, mos, budget, threads: (80.0, {"x": 1}))
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "2", "--warmup", "3"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "patterns/s"
+    assert line["value"] == pytest.approx(8 / 80.0)
+    assert line["e2e"] == {"value": line["value"], "unit": "patterns/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
