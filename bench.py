@@ -233,9 +233,11 @@ def max_over_ranks(values, world):
         return list(values)
     import torch
     import torch.distributed as dist
-    t = torch.tensor(values, dtype=torch.float64)
+    # NCCL reduces device tensors only; gloo (CPU tests) host tensors
+    device = f"cuda:{torch.cuda.current_device()}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor(values, dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return [float(x) for x in t]
+    return [float(x) for x in t.cpu()]
 
 
 def job_value(patterns_per_rank, steps, world, seconds):
