@@ -58,3 +58,51 @@ def test_cli_writes_reference_bytes(tmp_path):
     r = subprocess.run([exe, "14", *[str(x) for i in range(14) for x in (i, (i + 1) % 14)]], cwd=tmp_path,
                        capture_output=True, text=True)
     assert r.returncode != 0 and "core" in r.stderr
+
+
+def _random_connected(rng, n, extra):
+    """A random spanning tree on n vertices plus `extra` random edges."""
+    edges = set()
+    for v in range(1, n):
+        u = rng.randrange(v)
+        edges.add((u, v))
+    for _ in range(extra):
+        a, b = rng.randrange(n), rng.randrange(n)
+        if a != b:
+            edges.add((min(a, b), max(a, b)))
+    return sorted(edges)
+
+
+def test_random_patterns_against_the_reference_decomposer(tmp_path):
+    """Where the reference's own fringePreprocess was built from its sources
+    (oracle/_ref), 600 more seeded random patterns -- trees, sparse and dense
+    graphs of 2-24 vertices, relabelled at random -- decompose to the same
+    defined bytes, or are rejected by both."""
+    import random
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import oracle
+    from make_golden import defined_bytes
+    if not os.path.exists(oracle.REF_PREPROCESS):
+        pytest.skip("the reference's fringePreprocess is not built here")
+    rng = random.Random(20251207)
+    checked = rejected = 0
+    for i in range(600):
+        n = rng.randint(2, 24)
+        edges = _random_connected(rng, n, rng.choice([0, 1, 2, n // 2, n, 2 * n]))
+        perm = list(range(n))
+        rng.shuffle(perm)
+        edges = sorted((min(perm[a], perm[b]), max(perm[a], perm[b])) for a, b in edges)
+        args = [n] + [x for e in edges for x in e]
+        try:
+            want = defined_bytes(oracle.reference_preprocess(args, str(tmp_path))).hex()
+        except RuntimeError:
+            want = None
+        if want is None:
+            with pytest.raises(fsgc.FsgcError):
+                fsgc.preprocess(n, edges)
+            rejected += 1
+        else:
+            assert fsgc.preprocess(n, edges).to_bytes().hex() == want, (i, n, edges)
+            checked += 1
+    assert checked > 200 and rejected > 0  # dense draws often need a core above six vertices
