@@ -182,17 +182,7 @@ void pattern_csr(const fsgc_matching_order& mo, std::vector<long long>& off, std
   }
 }
 
-bool mo_valid(const fsgc_matching_order& mo) {
-  if (mo.nodes < 1 || mo.nodes > FSGC_MAX_CORE || mo.anchorsets > 63) return false;
-  int total = mo.nodes;
-  for (int i = 0; i < mo.anchorsets; i++) {
-    if (mo.anch[i] == 0 || mo.anch[i] >= (1 << mo.nodes)) return false;
-    total += mo.fcnt[i];
-  }
-  for (int i = 0; i + 1 < mo.nodes; i++)
-    if (mo.list[i] == 0 || mo.list[i] >= (2 << i)) return false;
-  return total <= FSGC_MAX_PATTERN;
-}
+bool mo_valid(const fsgc_matching_order& mo) { return fsgc::matching_order_valid(mo); }
 
 // The divisor for cores of 3+ vertices: the pattern counted in itself with the
 // same kernels.  The reference stores it in an int (src/fringeCount.cu:2213).
@@ -231,8 +221,9 @@ int automorphisms(fsgc_ctx* c, const fsgc_matching_order& mo, u64* out, int exac
   cudaStreamSynchronize(c->stream);
   free_graph(pg);
   if (st != FSGC_OK) return st;
-  const u64 aut = (u64)(unsigned int)(int)raw;
-  if (aut == 0) return fail(c, FSGC_EINVAL, "pattern has no match in itself");
+  uint64_t aut = 0;
+  if (fsgc_divisor_from_self_count(raw, &aut) != FSGC_OK)
+    return fail(c, FSGC_EINVAL, "the pattern's count in itself (%llu) is not a positive int: no divisor", raw);
   c->aut_cache[key] = aut;
   *out = aut;
   return FSGC_OK;
@@ -343,7 +334,37 @@ int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
 
 }  // namespace
 
+namespace fsgc {
+
+// A matching order the kernels can take: 1-6 core vertices, every later core
+// vertex joined to at least one earlier one (list[i] a non-empty subset of the
+// i+1 earlier vertices, so list[0] == 1), anchor sets non-empty subsets of the
+// core, at most 32 pattern vertices.
+bool matching_order_valid(const fsgc_matching_order& mo) {
+  if (mo.nodes < 1 || mo.nodes > FSGC_MAX_CORE || mo.anchorsets > 63) return false;
+  int total = mo.nodes;
+  for (int i = 0; i < mo.anchorsets; i++) {
+    if (mo.anch[i] == 0 || mo.anch[i] >= (1 << mo.nodes)) return false;
+    total += mo.fcnt[i];
+  }
+  for (int i = 0; i + 1 < mo.nodes; i++)
+    if (mo.list[i] == 0 || mo.list[i] >= (2 << i)) return false;
+  return total <= FSGC_MAX_PATTERN;
+}
+
+}  // namespace fsgc
+
 extern "C" {
+
+int fsgc_divisor_from_self_count(uint64_t self_count, uint64_t* out) {
+  if (!out) return FSGC_EINVAL;
+  *out = 0;
+  // the reference keeps the count in an int and asserts it is positive
+  const int as_int = (int)(unsigned int)(self_count & 0xffffffffULL);
+  if (as_int <= 0) return FSGC_EINVAL;
+  *out = (uint64_t)as_int;
+  return FSGC_OK;
+}
 
 int fsgc_ctx_create(int device, fsgc_ctx** out) {
   if (!out) return FSGC_EINVAL;

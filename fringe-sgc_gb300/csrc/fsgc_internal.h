@@ -95,6 +95,9 @@ struct DevWork {
 
 struct Launcher;  // forward
 
+// Structural checks of a matching order shared by every entry point (api.cu).
+bool matching_order_valid(const fsgc_matching_order& mo);
+
 // Entry points implemented in prep.cu / count.cu.
 int graph_degrees(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_scratch_u64);
 int prepare_graph(DevGraph& g, cudaStream_t s, uint64_t* launches, u64* d_scratch_u64);

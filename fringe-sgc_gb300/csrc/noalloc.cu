@@ -79,6 +79,7 @@ int fsgc_count_wedge_noalloc(int n, int64_t m, const int64_t* d_nindex, const in
   if (!mo || !out || n < 1 || m < 0 || !d_nindex || (m > 0 && !d_nlist))
     return set_err(errbuf, errlen, FSGC_EINVAL, "bad arguments");
   memset(out, 0, sizeof(*out));
+  if (!fsgc::matching_order_valid(*mo)) return set_err(errbuf, errlen, FSGC_EINVAL, "malformed matching order");
   // the wedge core with a fringe-free centre (src/fringeCount.cu:1783-1810)
   if (mo->nodes != 3 || __builtin_popcount(mo->list[1]) != 1 || mo->anchorsets < 1 || mo->anchorsets > 63)
     return set_err(errbuf, errlen, FSGC_EUNSUPPORTED, "only wedge-core patterns are supported");
@@ -200,8 +201,9 @@ int fsgc_count_wedge_noalloc(int n, int64_t m, const int64_t* d_nindex, const in
   u64 res[2] = {0, 0};
   NA_TRY(cudaMemcpyAsync(res, slots + S_RAW, 2 * sizeof(u64), cudaMemcpyDeviceToHost, s), "reading the count");
   NA_TRY(cudaStreamSynchronize(s), "count");
-  const u64 aut = (u64)(unsigned int)(int)res[1];
-  if (aut == 0) return set_err(errbuf, errlen, FSGC_EINVAL, "pattern has no match in itself");
+  uint64_t aut = 0;
+  if (fsgc_divisor_from_self_count(res[1], &aut) != FSGC_OK)
+    return set_err(errbuf, errlen, FSGC_EINVAL, "the pattern's count in itself is not a positive int: no divisor");
   out->raw_total = res[0];
   out->automorphisms = aut;
   out->count = res[0] / aut;

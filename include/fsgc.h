@@ -172,6 +172,13 @@ int fsgc_count_packed(fsgc_ctx* ctx, int gid, const fsgc_matching_order* mo, fsg
 /* ---- counting (replaces `fringeCount <graph> <motif.mo>`, src/fringeCount.cu:2265-2331,
  *      and occurrences(), :2199-2262) ---- */
 
+/* The divisor occurrences() takes from a pattern's count in itself
+ * (src/fringeCount.cu:2230-2232, 2250-2261): the reference stores that u64
+ * count in an int and asserts the int is positive.  *out = that int when it
+ * is positive; FSGC_EINVAL where the reference's assertion would stop the
+ * program (counts of cores with 3+ vertices then fail with FSGC_EINVAL). */
+int fsgc_divisor_from_self_count(uint64_t self_count, uint64_t* out);
+
 int fsgc_count(fsgc_ctx* ctx, int gid, const fsgc_matching_order* mo, fsgc_result* out);
 
 /* ---- exact counts (the reference has none: its u64 binomials wrap silently,
@@ -273,9 +280,18 @@ int fsgc_server_stats_get(fsgc_server* srv, fsgc_server_stats* out);
  * 64 MiB device array inside the library (held by each GPU that loads it until
  * the process exits); graphs that do not fit (about 16M vertices, fewer when
  * hub endpoints are large) and other pattern shapes return FSGC_EUNSUPPORTED.
+ * The caller's CSR is used as given, without the checks of the upload entry
+ * points: each list sorted ascending, no duplicates, no self loops, symmetric,
+ * every neighbour id in [0, n) (the reference's preconditions,
+ * src/fringeCount.cu:50-56).  Unsorted lists give a wrong count and no error;
+ * run fsgc_csr_validate on a host copy once if in doubt.
  * The first call on a device looks up that array's device address and loads a
- * constant table; make that first call before any stream capture.  All calls
- * share the array, so calls that overlap on the GPU race: serialise them. */
+ * constant table; make that first call before any stream capture.  Both stay
+ * valid for the life of the device's primary context: do not call this after
+ * a cudaDeviceReset on that device.  Each call reads the graph's maximum degree
+ * back to the host and waits for `stream` to finish the count before it
+ * returns.  All calls share the array, so calls that overlap on the GPU race:
+ * serialise them. */
 int fsgc_count_wedge_noalloc(int n, int64_t m, const int64_t* d_nindex, const int32_t* d_nlist,
                              const fsgc_matching_order* mo, void* stream, fsgc_result* out, char* errbuf,
                              int errlen);

@@ -799,9 +799,11 @@ int oracle_count(int n, const long long* idx, const int* adj, const unsigned cha
     }
     Graph pg{pn, pidx[pn], pidx.data(), padj.data()};
     aut = count_core<u64>(mo, pg, Sample(), &ct);
-    // the reference divides by an int (src/fringeCount.cu:2213, 2230)
-    aut = (u64)(unsigned int)(int)aut;
-    if (aut == 0) return -2;
+    // the reference keeps the divisor in an int and asserts it is positive
+    // (src/fringeCount.cu:2213, 2230-2232)
+    const int aut_int = (int)(unsigned int)(aut & 0xffffffffULL);
+    if (aut_int <= 0) return -2;
+    aut = (u64)aut_int;
   }
   const u64 raw = count_core<u64>(mo, g, s, &ct);
   out[0] = raw / aut;

@@ -18,9 +18,13 @@ REF_PREPROCESS = os.path.join(HERE, "_ref", "fringePreprocess")
 _lib = None
 
 
-def build():
-    """Compile the oracle (and, where the reference sources exist, its preprocessor)."""
-    subprocess.run(["make", "-s", "-C", HERE], check=True)
+def build(refsrc=None):
+    """Compile the oracle; with `refsrc` (the reference's src/ directory) also
+    the reference's own preprocessor and kernels into _ref/."""
+    cmd = ["make", "-s", "-C", HERE]
+    if refsrc:
+        cmd.append("REFSRC=" + refsrc)
+    subprocess.run(cmd, check=True)
 
 
 def lib():

@@ -347,13 +347,15 @@ struct Runner {
       DevGraph dpg = upload(pg);
       int c2;
       ull a2, r2;
-      aut = (ull)(unsigned)(int)occurrences(mo, dpg, false, &c2, &a2, &r2);
+      const int aut_int = (int)occurrences(mo, dpg, false, &c2, &a2, &r2);  // int automorphisms (:2230)
       R.set_u64(R.total, 0);
       R.set_int(R.wlsize, 0);
       R.set_int(R.wlpos, 0);
       R.set_int(R.maxdeg, 0);
       release(dpg);
-      if (aut == 0) { fprintf(stderr, "ref_runner: zero automorphisms\n"); exit(2); }
+      // assert(automorphisms > 0) (:2232)
+      if (aut_int <= 0) { fprintf(stderr, "ref_runner: automorphisms %d not positive\n", aut_int); exit(2); }
+      aut = (ull)aut_int;
     }
     *aut_out = aut;
     ull raw;

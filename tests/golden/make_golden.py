@@ -13,7 +13,7 @@ and records the bytes of motif.mo that the reference defines (undefined bytes
 of its uninitialised struct are stored as zero) or the rejection.
 
 Usage (where the reference tree is available):
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference
 """
 import json
 import os
@@ -105,8 +105,10 @@ def run(args, tmp):
 
 
 def main():
-    refroot = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    oracle.build()
+    if len(sys.argv) != 2 or not os.path.isdir(os.path.join(sys.argv[1], "src")):
+        raise SystemExit("usage: make_golden.py <reference tree> (the directory holding src/ and patterns/)")
+    refroot = sys.argv[1]
+    oracle.build(os.path.join(refroot, "src"))
     cases = []
     with tempfile.TemporaryDirectory() as tmp:
         for rel, n, pairs in corpus(refroot):

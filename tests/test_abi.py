@@ -102,3 +102,51 @@ def test_struct_layouts_match_the_header():
     assert C.sizeof(fsgc.Result) == 40
     assert C.sizeof(fsgc.ServerStats) == 64
     assert C.sizeof(fsgc.ExactResult) == 56
+
+
+def test_divisor_follows_the_references_int_and_assertion():
+    """occurrences() keeps a pattern's count in itself in an int and asserts it
+    is positive (src/fringeCount.cu:2230-2232): the divisor is that int, and a
+    self-count whose low 32 bits are zero or negative as an int is an error,
+    not a large positive divisor."""
+    import ctypes as C
+    L = fsgc.lib()
+    L.fsgc_divisor_from_self_count.restype = C.c_int
+    L.fsgc_divisor_from_self_count.argtypes = [C.c_ulonglong, C.POINTER(C.c_ulonglong)]
+    out = C.c_ulonglong()
+    for raw, want in [(1, 1), (24, 24), (2**31 - 1, 2**31 - 1), ((1 << 32) + 5, 5), ((7 << 40) + 12, 12)]:
+        assert L.fsgc_divisor_from_self_count(raw, C.byref(out)) == 0, raw
+        assert out.value == want
+    for raw in [0, 2**31, 2**32 - 1, (1 << 32) + 2**31 + 3, 1 << 32, 2**64 - 1]:
+        assert L.fsgc_divisor_from_self_count(raw, C.byref(out)) == 1, raw  # FSGC_EINVAL
+        assert out.value == 0
+    assert L.fsgc_divisor_from_self_count(1, None) == 1  # FSGC_EINVAL
+
+
+def test_standalone_graph_writer_equals_the_product_generator(tmp_path):
+    """oracle/graphgen (the reference arm's graph, written without the product
+    library) and fsgc_gen_rmat give the same .egr bytes."""
+    import refrun
+    for scale, ef, seed in [(9, 8, 1), (12, 16, 20251203), (14, 16, 20251203)]:
+        a, b = str(tmp_path / "a.egr"), str(tmp_path / "b.egr")
+        refrun.write_rmat_egr(a, scale, ef, 0.57, 0.19, 0.19, seed)
+        fsgc.egr_write(b, fsgc.gen_rmat(scale, ef, 0.57, 0.19, 0.19, seed))
+        assert open(a, "rb").read() == open(b, "rb").read(), (scale, ef, seed)
+        assert refrun.egr_header(a)[0] == 1 << scale
+
+
+def test_reference_arm_matching_orders_are_the_references():
+    """The reference arm takes the eight workload patterns' .mo bytes from the
+    reference CLI's own output; they equal fsgc_preprocess's."""
+    import refrun
+    sys_path_bench()
+    import bench
+    mos = refrun.workload_matching_orders(list(bench.WORKLOAD))
+    for name, (n, e) in bench.WORKLOAD.items():
+        assert mos[name] == fsgc.preprocess(n, e).to_bytes(), name
+
+
+def sys_path_bench():
+    import sys
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)

@@ -52,6 +52,29 @@ def test_noalloc_matches_regular_entry_point(graph):
         assert g.degrees().max() > 2048  # the hub-endpoint pass ran as well
 
 
+def test_noalloc_allocates_nothing_and_runs_on_the_callers_stream():
+    """After one warm-up call, a second call leaves the device's free memory
+    unchanged; the count is the same on a non-default stream."""
+    g = fsgc.gen_rmat(11, 8, seed=7)
+    d_idx = torch.from_numpy(g.nindex).cuda()
+    d_adj = torch.from_numpy(g.nlist).cuda()
+    mo = fsgc.preprocess(*PATTERNS["5-path"])
+    torch.cuda.synchronize()
+    first = fsgc.count_wedge_noalloc(g.n, g.m, d_idx.data_ptr(), d_adj.data_ptr(), mo)
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    again = fsgc.count_wedge_noalloc(g.n, g.m, d_idx.data_ptr(), d_adj.data_ptr(), mo)
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        on_side = fsgc.count_wedge_noalloc(g.n, g.m, d_idx.data_ptr(), d_adj.data_ptr(), mo,
+                                           stream=side.cuda_stream)
+    side.synchronize()
+    assert (first.count, first.raw_total) == (again.count, again.raw_total) == (on_side.count, on_side.raw_total)
+
+
 def test_noalloc_rejects_other_shapes():
     g = fsgc.gen_rmat(8, 4, seed=1)
     d_idx = torch.from_numpy(g.nindex).cuda()
@@ -62,3 +85,12 @@ def test_noalloc_rejects_other_shapes():
     centre = fsgc.preprocess(6, [(0, 1), (0, 2), (0, 3), (1, 4), (2, 5)])  # fringe on the centre
     with pytest.raises(fsgc.FsgcError):
         fsgc.count_wedge_noalloc(g.n, g.m, d_idx.data_ptr(), d_adj.data_ptr(), centre)
+    # malformed orders the regular entry point refuses: core vertex B not joined
+    # to A (list[0] == 0), and C joined to a vertex that does not precede it
+    wedge = fsgc.preprocess(5, [(0, 1), (0, 2), (1, 3), (2, 4)])
+    for pos, val in [(8, 0), (9, 4), (9, 0)]:
+        b = bytearray(wedge.to_bytes())
+        b[pos] = val
+        bad = fsgc.MatchingOrder.from_bytes(bytes(b))
+        with pytest.raises(fsgc.FsgcError):
+            fsgc.count_wedge_noalloc(g.n, g.m, d_idx.data_ptr(), d_adj.data_ptr(), bad)
