@@ -135,7 +135,9 @@ int upload_graph(fsgc_ctx* c, int n, long long m, const long long* off, const in
   g->n = n;
   g->m = m;
   cudaError_t e = cudaMalloc((void**)&g->off, sizeof(long long) * ((size_t)n + 1));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&g->adj, sizeof(int) * (size_t)std::max(1LL, m));
+  // the neighbour lists are padded by 16 bytes: bulk copies into shared memory
+  // round a list's end up to a 16-byte boundary
+  if (e == cudaSuccess) e = cudaMalloc((void**)&g->adj, sizeof(int) * (size_t)std::max(1LL, m) + 16);
   if (e == cudaSuccess) e = cudaMalloc((void**)&g->deg, sizeof(int) * (size_t)std::max(1, n));
   if (e != cudaSuccess) {
     free_graph(g);
@@ -213,6 +215,8 @@ int automorphisms(fsgc_ctx* c, const fsgc_matching_order& mo, u64* out, int exac
       cudaMemcpyAsync(c->h_slots, c->d_slots, sizeof(u64), cudaMemcpyDeviceToHost, c->stream);
       cudaError_t e = cudaStreamSynchronize(c->stream);
       if (e != cudaSuccess) st = cuda_fail(c, e, "automorphism count");
+      else if (fsgc::take_kernel_error(c->work, c->stream) != FSGC_OK)
+        st = fail(c, FSGC_ETIMEDOUT, "the automorphism count's kernel gave up a bounded wait");
       raw = c->h_slots[0];
     }
   } else {
@@ -328,11 +332,25 @@ int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
   st = enqueue_tasks(c, tasks, nt, c->stream, c->work, c->d_slots, c->h_slots, c->events.data(), jobs, res, false);
   if (st != FSGC_OK) return st;
   CK(cudaStreamSynchronize(c->stream), "count");
+  st = fsgc::take_kernel_error(c->work, c->stream);
+  if (st != FSGC_OK) return fail(c, st, "a counting kernel gave up a bounded wait; the counts are void");
   for (int t = 0; t < nt; t++) finish_task(t, jobs, aut, c->h_slots, c->events.data(), res);
   return FSGC_OK;
 }
 
 }  // namespace
+
+namespace fsgc {
+
+int take_kernel_error(DevWork& w, cudaStream_t s) {
+  if (!w.h_err || *w.h_err == 0) return FSGC_OK;
+  *w.h_err = 0;
+  cudaMemsetAsync(w.small + kErrWord, 0, sizeof(u64), s);
+  cudaStreamSynchronize(s);
+  return FSGC_ETIMEDOUT;
+}
+
+}  // namespace fsgc
 
 namespace fsgc {
 
@@ -386,12 +404,14 @@ int fsgc_ctx_create(int device, fsgc_ctx** out) {
     }
   }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc((void**)&c->work.small, 32 * sizeof(u64)) != cudaSuccess || ensure_slots(c, 64) != FSGC_OK) {
+      cudaMalloc((void**)&c->work.small, 32 * sizeof(u64)) != cudaSuccess ||
+      cudaMallocHost((void**)&c->work.h_err, sizeof(u64)) != cudaSuccess || ensure_slots(c, 64) != FSGC_OK) {
     cudaGetLastError();
     fsgc_ctx_destroy(c);
     return FSGC_ECUDA;
   }
   cudaMemset(c->work.small, 0, 32 * sizeof(u64));
+  *c->work.h_err = 0;
   if (cudaDeviceSynchronize() != cudaSuccess) {
     // kernels for this architecture missing or device unusable
     cudaGetLastError();
@@ -413,6 +433,7 @@ void fsgc_ctx_destroy(fsgc_ctx* c) {
   if (c->t1) cudaEventDestroy(c->t1);
   cudaFree(c->flush_buf);
   cudaFree(c->work.small);
+  cudaFreeHost(c->work.h_err);
   cudaFree(c->work.tri.ptr);
   cudaFree(c->d_slots);
   cudaFreeHost(c->h_slots);
@@ -645,6 +666,8 @@ int fsgc_count_packed(fsgc_ctx* c, int gid, const fsgc_matching_order* mo, fsgc_
   CK(cudaEventRecord(c->events[1], c->stream), "event");
   CK(cudaMemcpyAsync(c->h_member, c->d_member, sizeof(u64) * (size_t)ng, cudaMemcpyDeviceToHost, c->stream), "readback");
   CK(cudaStreamSynchronize(c->stream), "packed count");
+  st = fsgc::take_kernel_error(c->work, c->stream);
+  if (st != FSGC_OK) return fail(c, st, "a counting kernel gave up a bounded wait; the counts are void");
   float ms = 0;
   cudaEventElapsedTime(&ms, c->events[0], c->events[1]);
   for (int i = 0; i < ng; i++) {
@@ -728,6 +751,8 @@ int fsgc_count_exact(fsgc_ctx* c, int gid, const fsgc_matching_order* mo, fsgc_e
   CK(cudaEventRecord(c->events[1], c->stream), "event");
   CK(cudaMemcpyAsync(c->h_slots, c->d_slots, 3 * sizeof(u64), cudaMemcpyDeviceToHost, c->stream), "readback");
   CK(cudaStreamSynchronize(c->stream), "exact count");
+  st = fsgc::take_kernel_error(c->work, c->stream);
+  if (st != FSGC_OK) return fail(c, st, "a counting kernel gave up a bounded wait; the count is void");
   unsigned __int128 raw;
   bool sat = false;
   if (job.host_only) {
@@ -783,6 +808,8 @@ int fsgc_lane_create(fsgc_ctx* c, fsgc_lane** out) {
   L->ctx = c;
   cudaError_t e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc((void**)&L->work.small, 32 * sizeof(u64));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&L->work.h_err, sizeof(u64));
+  if (e == cudaSuccess) *L->work.h_err = 0;
   if (e == cudaSuccess) e = cudaMemsetAsync(L->work.small, 0, 32 * sizeof(u64), L->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
   if (e != cudaSuccess) {
@@ -800,6 +827,7 @@ void fsgc_lane_destroy(fsgc_lane* L) {
   if (L->stream) cudaStreamSynchronize(L->stream);
   for (auto e : L->events) cudaEventDestroy(e);
   cudaFree(L->work.small);
+  cudaFreeHost(L->work.h_err);
   cudaFree(L->work.tri.ptr);
   cudaFree(L->d_slots);
   cudaFreeHost(L->h_slots);
@@ -859,6 +887,13 @@ int fsgc_lane_wait_task(fsgc_lane* L, int index, fsgc_result* out) {
     L->pending = 0;
     std::lock_guard<std::mutex> lk(L->ctx->mu);
     return cuda_fail(L->ctx, e, "lane count");
+  }
+  if (L->work.h_err && *L->work.h_err) {
+    // a kernel of this submission gave up a bounded wait: its counts are void
+    L->pending = 0;
+    fsgc::take_kernel_error(L->work, L->stream);
+    std::lock_guard<std::mutex> lk(L->ctx->mu);
+    return fail(L->ctx, FSGC_ETIMEDOUT, "a counting kernel gave up a bounded wait; the counts are void");
   }
   for (int t = L->finished; t <= index; t++) finish_task(t, L->jobs, L->aut, L->h_slots, L->events.data(), L->res.data());
   L->finished = index + 1;

@@ -216,6 +216,7 @@ struct TriParams {
   int tails;
   int relabel;  // roles by (deg, id) order (1) or by id (0)
   int kmax;     // largest out-degree (bitmap kernel)
+  int stage;    // bitmap kernel: longest N(a) staged in shared memory (ints, multiple of 32)
   Rot3 rot;
 };
 
@@ -370,23 +371,41 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
 
 // Triangle core, general placements: one block per vertex a, handling every
 // triangle whose lowest (deg, id) vertex is a.  For each out-neighbour b_i of a
-// the block builds the bitmap M_i of N(a) & N(b_i) over the positions of N(a)
-// (one warp ballot per 32 neighbours).  Then a pair (b_i, b_j) is a triangle
-// iff bit pos(b_j) of M_i is set, |N(a) & N(b_i)| = popc(M_i), and the triple
-// overlap |N(a) & N(b_i) & N(b_j)| = popc(M_i & M_j) -- a few word operations
-// per triangle instead of an intersection of full neighbour lists.
+// the block builds the bitmap M_i of N(a) & N(b_i) over the positions of N(a).
+// Then a pair (b_i, b_j) is a triangle iff bit pos(b_j) of M_i is set,
+// |N(a) & N(b_i)| = popc(M_i), and the triple overlap |N(a) & N(b_i) & N(b_j)|
+// = popc(M_i & M_j) -- a few word operations per triangle instead of an
+// intersection of full neighbour lists.
+//
+// N(a) is staged in shared memory by a bulk copy when it fits p.stage ints.  A
+// row then takes the cheaper of two ways: walk N(b_i) from global memory
+// (coalesced) and look each entry up in the staged N(a), building the row in
+// a per-warp shared buffer, when deg b_i <= kTriWalkRatio * deg a; otherwise
+// test each entry of N(a) by a binary search of N(b_i) (one ballot per 32).
+constexpr int kTriWalkRatio = 16;
+constexpr int kTriThreads = 256;
+constexpr int kBulkWaitPolls = 1 << 22;  // bounded wait for a bulk copy
+
 template <class A>
-__global__ void __launch_bounds__(256, 3) triangle_bitmap_kernel(GView g, TriParams p, int* __restrict__ queue,
-                                                              unsigned* __restrict__ bits_all, long long bits_per_block,
-                                                              u64* __restrict__ slot) {
-  extern __shared__ int s_dyn[];
+__global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g, TriParams p, int* __restrict__ queue,
+                                                                      unsigned* __restrict__ bits_all,
+                                                                      long long bits_per_block,
+                                                                      unsigned long long* __restrict__ err,
+                                                                      u64* __restrict__ slot) {
+  extern __shared__ __align__(16) int s_dyn[];
   __shared__ int s_a;
+  __shared__ __align__(8) unsigned long long s_bar;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   unsigned* bits = bits_all + (size_t)blockIdx.x * (size_t)bits_per_block;
-  const int kmax = p.kmax;
-  int* outl = s_dyn;            // out-neighbours of a
-  int* pos = s_dyn + kmax;      // their positions in N(a)
-  int* rowpop = s_dyn + 2 * kmax;  // |N(a) & N(b_i)|
+  const int kmax = p.kmax, stage = p.stage;
+  int* s_na = s_dyn;                              // staged N(a): stage + 4 ints (16-byte aligned)
+  unsigned* s_row = reinterpret_cast<unsigned*>(s_dyn + stage + 4);  // per warp: stage / 32 words
+  int* outl = s_dyn + stage + 4 + (stage >> 5) * (kTriThreads >> 5);  // out-neighbours of a
+  int* pos = outl + kmax;                         // their positions in N(a)
+  int* rowpop = outl + 2 * kmax;                  // |N(a) & N(b_i)|
+  unsigned parity = 0;
+  if (threadIdx.x == 0 && stage > 0) mbar_init(&s_bar, 1);
+  __syncthreads();
   A acc = A(0);
   for (;;) {
     if (threadIdx.x == 0) s_a = atomicAdd(queue, 1);
@@ -398,29 +417,71 @@ __global__ void __launch_bounds__(256, 3) triangle_bitmap_kernel(GView g, TriPar
     const int da = g.deg[a];
     if (k >= 2 && da >= p.sum1) {
       const int W = (da + 31) >> 5;
-      const int* Na = g.adj + g.off[a];
+      const long long abeg = g.off[a];
+      const bool staged = da <= stage;
+      const int* Na = g.adj + abeg;
+      if (staged) {
+        // the copy starts at the 16-byte boundary at or below N(a) (the list
+        // array is padded by 16 bytes, so the rounded-up end stays inside it)
+        const long long cbeg = abeg & ~3LL;
+        const int shift = (int)(abeg - cbeg);
+        if (threadIdx.x == 0) {
+          fence_proxy_async_smem();
+          const unsigned bytes = (unsigned)(((shift + da) * 4 + 15) & ~15);
+          bulk_copy_g2s(s_na, g.adj + cbeg, bytes, &s_bar);
+        }
+        const bool done = mbar_wait_bounded(&s_bar, parity, kBulkWaitPolls);
+        parity ^= 1u;
+        if (__syncthreads_or(!done)) {
+          // the copy did not complete: report it, give the copy one more
+          // bounded wait and leave (the count is void)
+          if (threadIdx.x == 0) atomicOr(err, 1ULL);
+          mbar_wait_bounded(&s_bar, parity ^ 1u, kBulkWaitPolls);
+          return;
+        }
+        Na = s_na + shift;
+      }
       for (int i = threadIdx.x; i < k; i += blockDim.x) {
         const int b = g.oadj[ob + i];
         outl[i] = b;
         pos[i] = lower_bound_dev(Na, da, b);
+        rowpop[i] = (int)g.osup[ob + i];  // |N(a) & N(b_i)| is the edge's support
       }
       // bitmaps: row i = N(a) & N(b_i), skipped when the edge closes no triangle
+      unsigned* wrow = s_row + warp * (stage >> 5);
       for (int i = warp; i < k; i += nwarp) {
-        const unsigned sup = g.osup[ob + i];
-        int cnt = 0;
-        if (sup) {
-          const int b = g.oadj[ob + i];
-          const int* Nb = g.adj + g.off[b];
-          const int db = g.deg[b];
+        if (g.osup[ob + i] == 0) continue;
+        const int b = g.oadj[ob + i];
+        const int* Nb = g.adj + g.off[b];
+        const int db = g.deg[b];
+        unsigned* row = bits + (size_t)i * W;
+        if (staged && db <= kTriWalkRatio * da) {
+          for (int w = lane; w < W; w += 32) wrow[w] = 0u;
+          __syncwarp();
+          // only N(b) entries inside [min N(a), max N(a)] can match
+          const int t0 = lower_bound_dev(Nb, db, Na[0]);
+          const int t1 = lower_bound_dev(Nb, db, Na[da - 1] + 1);
+          for (int t = t0 + lane; t < t1; t += 32) {
+            const int y = __ldg(Nb + t);
+            int lo = 0, hi = da;  // y's position in the staged N(a)
+            while (lo < hi) {
+              const int mid = (lo + hi) >> 1;
+              if (Na[mid] < y) lo = mid + 1;
+              else hi = mid;
+            }
+            if (lo < da && Na[lo] == y) atomicOr(&wrow[lo >> 5], 1u << (lo & 31));
+          }
+          __syncwarp();
+          for (int w = lane; w < W; w += 32) row[w] = wrow[w];
+          __syncwarp();
+        } else {
           for (int w = 0; w < W; w++) {
             const int x = w * 32 + lane;
-            const bool hit = (x < da) && bsearch_has(Nb, db, __ldg(Na + x));
+            const bool hit = (x < da) && bsearch_has(Nb, db, Na[x]);
             const unsigned word = __ballot_sync(0xffffffffu, hit);
-            if (lane == 0) bits[(size_t)i * W + w] = word;
-            cnt += __popc(word);
+            if (lane == 0) row[w] = word;
           }
         }
-        if (lane == 0) rowpop[i] = cnt;
       }
       __syncthreads();
       // pairs (i, j), i < j: warp per row, lanes over j
@@ -518,6 +579,31 @@ struct WedgeCfg {
   static constexpr int TW = WORDS / 32;            // touched-bitmap words (= kWThreads)
   static constexpr int CH_MAX = BIG ? CH : 4 * CH; // widest chunk (4-bit counters)
 };
+
+// One bit, the lowest of the counter, for every non-zero `bits`-wide counter of
+// `word` (bits = 4, 8, 16 or 32): each counter's bits are OR-folded into its
+// lowest bit.
+__device__ __forceinline__ unsigned nonzero_counter_bits(unsigned word, int bits) {
+  if (bits == 32) return word != 0u ? 1u : 0u;
+  unsigned t = word;
+  for (int s = bits >> 1; s > 0; s >>= 1) t |= t >> s;
+  return t & (bits == 16 ? 0x00010001u : (bits == 8 ? 0x01010101u : 0x11111111u));
+}
+
+// Position of the n-th (from 0) set bit of mask, which has more than n set
+// bits: a halving search on the population counts of the low halves.
+__device__ __forceinline__ int nth_set_bit(unsigned mask, int n) {
+  int pos = 0;
+  for (int w = 16; w >= 1; w >>= 1) {
+    const int c = __popc(mask & ((1u << w) - 1u));
+    if (n >= c) {
+      n -= c;
+      mask >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
 
 // counter width for an owner of degree dv (SMALL kernel)
 __device__ __forceinline__ int wedge_counter_bits(int dv) { return dv <= 15 ? 4 : (dv <= 255 ? 8 : 16); }
@@ -704,8 +790,11 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
         }
       }
       __syncthreads();
-      // evaluate: prefix-sum the touched-word popcounts (one bitmap word per
-      // thread) and give every thread an equal share of the touched words
+      // evaluate: the chunk's touched counter words are split evenly over the
+      // warps (a prefix over the touched-bitmap words); a warp loads 32 words
+      // at a time, one per lane, prefix-sums their non-zero counters and then
+      // hands out one (endpoint, centre count) pair per lane per step, so the
+      // lanes evaluate in lockstep and adjacent lanes take adjacent endpoints.
       {
         const int nw = (hi - lo + (1 << lper) - 1) >> lper;
         const int ntw = (nw + 31) >> 5;
@@ -731,34 +820,48 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
         S.tpre[tid] = S.warp_tmp[warp] + inc - c0;
         const int T = S.warp_tmp[32];
         __syncthreads();
-        const int r0 = (int)(((long long)T * tid) / blockDim.x), r1 = (int)(((long long)T * (tid + 1)) / blockDim.x);
-        if (r0 < r1) {
-          int a = 0, b = ntw;  // bitmap word holding rank r0: last with tpre <= r0
-          while (b - a > 1) {
-            const int mid = (a + b) >> 1;
-            if (S.tpre[mid] <= r0) a = mid;
-            else b = mid;
+        const int W0 = (int)(((long long)T * warp) / nwarp), W1 = (int)(((long long)T * (warp + 1)) / nwarp);
+        const int lbits = BIG ? 5 : (lper == 1 ? 4 : (lper == 2 ? 3 : 2));  // log2(bits)
+        const unsigned cmask = BIG ? 0xffffffffu : ((1u << bits) - 1);
+        for (int W = W0; W < W1; W += 32) {
+          const int idx = W + lane;
+          int wd = 0, c = 0;
+          unsigned word = 0, nz = 0;
+          if (idx < W1) {
+            int a = 0, b = ntw;  // bitmap word holding touched word `idx`: last with tpre <= idx
+            while (b - a > 1) {
+              const int mid = (a + b) >> 1;
+              if (S.tpre[mid] <= idx) a = mid;
+              else b = mid;
+            }
+            wd = (a << 5) + nth_set_bit(S.touched[a], idx - S.tpre[a]);
+            word = S.cnt[wd];
+            nz = nonzero_counter_bits(word, bits);
+            c = __popc(nz);
           }
-          unsigned mask = S.touched[a];
-          for (int k = r0 - S.tpre[a]; k > 0; k--) mask &= mask - 1;
-          for (int r = r0; r < r1; r++) {
-            while (mask == 0) mask = S.touched[++a];
-            const int wd = (a << 5) + (__ffs(mask) - 1);
-            mask &= mask - 1;
-            const unsigned word = S.cnt[wd];
-            S.cnt[wd] = 0;
-            if (BIG) {
-              const int w = lo + wd;
-              eval_pair<BIG, A>(g, p, S, lo, wd, word, g.deg[w], v, dv, thres, acc);
-            } else {
-              const int o0 = wd << lper;
-              const unsigned cmask = (1u << (bits & 31)) - 1;  // bits is 4, 8 or 16 here
-              for (unsigned rest = word; rest; ) {
-                const int k = (__ffs(rest) - 1) / bits;  // next non-zero counter of the word
-                const unsigned C = (word >> (k * bits)) & cmask;
-                rest &= ~(cmask << (k * bits));
-                eval_pair<BIG, A>(g, p, S, lo, o0 + k, C, g.deg[lo + o0 + k], v, dv, thres, acc);
-              }
+          int incl = c;
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int excl = incl - c;
+          const int P = __shfl_sync(0xffffffffu, incl, 31);
+          for (int q = 0; q < P; q += 32) {
+            const int i = q + lane;
+            int s = 0;  // source lane: the last with excl <= i
+            for (int step = 16; step >= 1; step >>= 1) {
+              const int e = __shfl_sync(0xffffffffu, excl, s + step);
+              if (e <= i) s += step;
+            }
+            const int wdS = __shfl_sync(0xffffffffu, wd, s);
+            const unsigned wordS = __shfl_sync(0xffffffffu, word, s);
+            const unsigned nzS = __shfl_sync(0xffffffffu, nz, s);
+            const int exS = __shfl_sync(0xffffffffu, excl, s);
+            if (i < P) {
+              const int kbit = nth_set_bit(nzS, i - exS);  // low bit of the counter
+              const unsigned C = (wordS >> kbit) & cmask;
+              const int o = (wdS << lper) + (kbit >> lbits);
+              eval_pair<BIG, A>(g, p, S, lo, o, C, g.deg[lo + o], v, dv, thres, acc);
             }
           }
         }
@@ -773,7 +876,10 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
       nxt = __reduce_min_sync(0xffffffffu, nxt);
       if (tid == 0) S.lo = v;
       __syncthreads();  // touched, adjbits, pre and S.lo are free again
-      for (int i = tid; i < TW; i += blockDim.x) S.touched[i] = 0;
+      for (int i = tid; i < TW; i += blockDim.x) {
+        for (unsigned mk = S.touched[i]; mk; mk &= mk - 1) S.cnt[(i << 5) + __ffs(mk) - 1] = 0;
+        S.touched[i] = 0;
+      }
       for (int i = cs + tid; i < cend; i += blockDim.x) S.adjbits[(__ldg(Nv + i) - lo) >> 5] = 0;
       cv = cend;
       if (lane == 0 && nxt < v) atomicMin(&S.lo, max(hi, (nxt / CH) * CH));
@@ -926,6 +1032,7 @@ struct GenParams {
   uint8_t destdeg[5];
   uint8_t list[5];
   int nslots;
+  int lane_venn_max;  // a lane builds its own match's Venn row up to this many list entries
   uint8_t slot_idx[kMaxSlots];  // region bitmap of each placement step
   uint8_t slot_set[kMaxSlots];  // anchor set index of each step
   uint8_t slot_top[kMaxSlots];  // 1 if the step takes all remaining fringes
@@ -935,21 +1042,23 @@ struct GenParams {
   int exact;  // 1: exact placement sum; 0: the reference's functionX
 };
 
-// Placement sum (functionX, src/fringeCount.cu:408-486) over the precomputed
-// step list: step s puts a fringes of its anchor set into region slot_idx[s];
-// the last step of each set takes all its remaining fringes.  Each complete
-// placement adds the product of nck(remaining region size, fringes placed).
-template <class A>
+// Placement sum over the precomputed step list (exact count of placements):
+// step s puts a fringes of its anchor set into region slot_idx[s]; the last
+// step of each set takes all its remaining fringes.  Each complete placement
+// adds the product of nck(remaining region size, fringes placed).  D bounds
+// the number of steps (the host picks the smallest D >= nslots); per step the
+// walk keeps the fringes placed, those left and the partial product.
+template <int D, class A>
 __device__ A placement_sum(const GenParams& p, int* venn) {
-  int a_[kMaxSlots];
-  int rem_[kMaxSlots];
-  A pre_[kMaxSlots];
+  int8_t a_[D];
+  uint8_t rem_[D];
+  A pre_[D];
   const int S = p.nslots;
   A sum = A(0);
   int s = 0;
   rem_[0] = p.fcnt[p.slot_set[0]];
   pre_[0] = A(1);
-  a_[0] = p.slot_top[0] ? rem_[0] : min(venn[p.slot_idx[0]], rem_[0]);
+  a_[0] = (int8_t)(p.slot_top[0] ? rem_[0] : min(venn[p.slot_idx[0]], (int)rem_[0]));
   while (s >= 0) {
     if (a_[s] < 0) {  // this step is exhausted: back up
       s--;
@@ -969,44 +1078,48 @@ __device__ A placement_sum(const GenParams& p, int* venn) {
     venn[idx] -= a_[s];
     const int ns = s + 1;
     pre_[ns] = w;
-    rem_[ns] = p.slot_top[s] ? (int)p.fcnt[p.slot_set[ns]] : rem_[s] - a_[s];
-    a_[ns] = p.slot_top[ns] ? rem_[ns] : min(venn[p.slot_idx[ns]], rem_[ns]);
+    rem_[ns] = (uint8_t)(p.slot_top[s] ? (int)p.fcnt[p.slot_set[ns]] : rem_[s] - a_[s]);
+    a_[ns] = (int8_t)(p.slot_top[ns] ? rem_[ns] : min(venn[p.slot_idx[ns]], (int)rem_[ns]));
     s = ns;
   }
   return sum;
 }
 
 // functionX with the reference's own control flow (src/fringeCount.cu:408-486),
-// the default: a flat depth-first walk that saves (a, prod, region,
-// venn[region], fr[set]) per level and, when it backs up, restores only the
-// level it returns to.  A region changed by the step it abandons keeps that
-// change, so later alternatives can see it reduced; for anchor sets with two
-// or more fringes the sum then differs from placement_sum (the exact count),
-// and the reference's counts are these sums.
+// the default: a flat depth-first walk that saves (a, prod, venn[region],
+// fr[set]) per level and, when it backs up, restores only the level it returns
+// to.  A region changed by the step it abandons keeps that change, so later
+// alternatives can see it reduced; for anchor sets with two or more fringes
+// the sum then differs from placement_sum (the exact count), and the
+// reference's counts are these sums.  Level s is step s of the host's step
+// list, so the region and anchor set of a level come from the table instead of
+// the saved state, and D (>= nslots, chosen on the host) bounds the depth:
+// 14 bytes of state per level instead of the reference's 21 x 665.
+template <int D>
 __device__ u64 placement_sum_reference(const GenParams& p, int* venn) {
-  int savea[kMaxSlots], savevenn[kMaxSlots];
-  u64 saveprod[kMaxSlots];
-  uint8_t saveidx[kMaxSlots], savefr[kMaxSlots];
+  int8_t savea[D];
+  uint8_t savefr[D];
+  int savevenn[D];
+  u64 saveprod[D];
   uint8_t fr[64];
   for (int i = 0; i < 64; i++) fr[i] = 0;
   for (int i = 0; i < p.nsets; i++) fr[p.anch[i]] = p.fcnt[i];
-  const int top = p.anchors, non = p.nonanchors;
-  int asi = p.nsets - 1;
   u64 sum = 0, prod = 1;
   int level = 0;
-  int anch = p.anch[asi];
-  int idx = anch;
-  int a = min(venn[idx], (int)fr[anch]);
+  int a = min(venn[p.slot_idx[0]], (int)fr[p.anch[p.slot_set[0]]]);
   for (;;) {
-    savea[level] = a; saveprod[level] = prod; saveidx[level] = (uint8_t)idx;
+    const int idx = p.slot_idx[level];
+    const int anch = p.anch[p.slot_set[level]];
+    const bool top = p.slot_top[level] != 0;
+    savea[level] = (int8_t)a; saveprod[level] = prod;
     savevenn[level] = venn[idx]; savefr[level] = fr[anch];
     if (a < 0) {
       prod = 0;
-    } else if (idx == top) {
+    } else if (top) {
       prod *= nck(venn[idx], fr[anch]);
       venn[idx] -= fr[anch];
       fr[anch] = 0;
-      if (asi == 0) { sum += prod; prod = 0; }
+      if (p.slot_set[level] == 0) { sum += prod; prod = 0; }
     } else {
       prod *= nck(venn[idx], a);
       venn[idx] -= a;
@@ -1017,74 +1130,117 @@ __device__ u64 placement_sum_reference(const GenParams& p, int* venn) {
       if (level < 0) break;
       a = savea[level] - 1;
       prod = saveprod[level];
-      idx = saveidx[level];
-      if (idx == top) { asi++; anch = p.anch[asi]; }
-      venn[idx] = savevenn[level];
-      fr[anch] = savefr[level];
+      venn[p.slot_idx[level]] = savevenn[level];
+      fr[p.anch[p.slot_set[level]]] = savefr[level];
     } else {
       level++;
-      if (idx == top) { asi--; anch = p.anch[asi]; idx = anch; }
-      else idx = (((idx | non) + 1) | anch) & ~non;
-      a = (idx == top) ? 0 : min(venn[idx], (int)fr[anch]);
+      const int nidx = p.slot_idx[level];
+      a = p.slot_top[level] ? 0 : min(venn[nidx], (int)fr[p.anch[p.slot_set[level]]]);
     }
   }
   return sum;
 }
 
 constexpr int kGenWarps = 4;  // warps per block in the general-core kernel
+constexpr int kGenLaneVennMax = 96;  // list entries up to which a lane builds its own Venn row
 
 struct GenWarp {
   int stack[6];
-  int venn[32][64];  // one Venn row per lane (the lane that owns the match)
+  int venn[32][65];  // one Venn row per lane (the lane that owns the match); padded against bank conflicts
 };
 
-// exclusive Venn sizes of the current match into row[]; warp-cooperative
-__device__ void venn_general(const GView& g, const GenParams& p, const int* stack, int* row) {
-  const int lane = threadIdx.x & 31;
-  const int top = 1 << p.k;
-  for (int i = lane; i < 64; i += 32) row[i] = 0;
-  __syncwarp();
-  // each neighbour x of an anchor is counted once, from the lowest anchor it
-  // touches, under the exact set of anchors it touches
+// Exclusive Venn regions of one core match: row[S] = number of vertices whose
+// set of adjacent anchor core vertices is exactly S, minus the core vertices
+// themselves (commonX, src/fringeCount.cu:345-405, computes the same sizes by
+// inclusion-exclusion over every anchor's full list).  Here the anchor with the
+// longest list, M, is never walked: every vertex adjacent to M and to another
+// anchor is counted from the first other anchor (in core order) it touches,
+// and row[{M}] = deg M - those.  Each walked entry needs one membership test
+// per other anchor.  `vert(i)` gives the match's vertex at core position i.
+// Warp-cooperative (LANES = 32, atomics into row) or by one lane (LANES = 1).
+template <int LANES, class VertOf>
+__device__ void venn_exclusive(const GView& g, const GenParams& p, VertOf vert, int* row) {
+  const int lane = (LANES == 1) ? 0 : (threadIdx.x & 31);
+  for (int i = lane; i < 64; i += LANES) row[i] = 0;
+  if (LANES > 1) __syncwarp();
+  int big = -1, bigdeg = -1;
+  for (int i = 0; i < p.k; i++)
+    if (p.anchors & (1 << i)) {
+      const int d = g.deg[vert(i)];
+      if (d >= bigdeg) { big = i; bigdeg = d; }
+    }
   for (int i = 0; i < p.k; i++) {
-    if (!(p.anchors & (1 << i))) continue;
-    const int vi = stack[i];
+    if (!(p.anchors & (1 << i)) || i == big) continue;
+    const int vi = vert(i);
     const long long b = g.off[vi];
     const int d = (int)(g.off[vi + 1] - b);
-    for (int t = lane; t < d; t += 32) {
+    for (int t = lane; t < d; t += LANES) {
       const int x = __ldg(g.adj + b + t);
       int bmp = 1 << i;
       bool first = true;
       for (int q = 0; q < p.k && first; q++) {
         if (q == i || !(p.anchors & (1 << q))) continue;
-        const int vq = stack[q];
+        const int vq = vert(q);
         const long long qb = g.off[vq];
         if (bsearch_has(g.adj + qb, (int)(g.off[vq + 1] - qb), x)) {
-          if (q < i) first = false;
+          if (q < i && q != big) first = false;  // counted from anchor q
           else bmp |= 1 << q;
         }
       }
-      if (first) atomicAdd(row + bmp, 1);
+      if (first) {
+        if (LANES > 1) atomicAdd(row + bmp, 1);
+        else row[bmp]++;
+      }
     }
   }
-  __syncwarp();
+  if (LANES > 1) __syncwarp();
+  if (lane == 0) {
+    int shared_with_big = 0;
+    for (int s = 1; s < 64; s++)
+      if ((s & (1 << big)) && s != (1 << big)) shared_with_big += row[s];
+    row[1 << big] = bigdeg - shared_with_big;
+  }
+  if (LANES > 1) __syncwarp();
   // core vertices themselves are not fringe candidates
-  if (lane < p.k) {
-    const int x = stack[lane];
+  for (int c = lane; c < p.k; c += LANES) {
+    const int x = vert(c);
     int bmp = 0;
     for (int q = 0; q < p.k; q++) {
       if (!(p.anchors & (1 << q))) continue;
-      const int vq = stack[q];
+      const int vq = vert(q);
       const long long qb = g.off[vq];
       if (bsearch_has(g.adj + qb, (int)(g.off[vq + 1] - qb), x)) bmp |= 1 << q;
     }
-    if (bmp) atomicSub(row + bmp, 1);
+    if (bmp) {
+      if (LANES > 1) atomicSub(row + bmp, 1);
+      else row[bmp]--;
+    }
   }
-  __syncwarp();
-  (void)top;
+  if (LANES > 1) __syncwarp();
 }
 
-template <int L, class A>
+// Entries a Venn row walks: the anchors' lists except the longest.
+template <class VertOf>
+__device__ __forceinline__ int venn_walk_len(const GView& g, const GenParams& p, VertOf vert) {
+  int sum = 0, big = 0;
+  for (int i = 0; i < p.k; i++)
+    if (p.anchors & (1 << i)) {
+      const int d = g.deg[vert(i)];
+      sum += d;
+      big = max(big, d);
+    }
+  return sum - big;
+}
+
+template <int D, class A>
+__device__ __forceinline__ A placement_of(const GenParams& p, int* row) {
+  if constexpr (std::is_same<A, u64>::value)
+    return p.exact ? placement_sum<D, u64>(p, row) : placement_sum_reference<D>(p, row);
+  else
+    return placement_sum<D, A>(p, row);  // exact counts: exact placements
+}
+
+template <int L, int D, class A>
 __device__ A gen_level(const GView& g, const GenParams& p, GenWarp& w) {
   // choose stack[L+1] among the neighbours of the first core vertex it must touch
   const int lane = threadIdx.x & 31;
@@ -1114,62 +1270,81 @@ __device__ A gen_level(const GView& g, const GenParams& p, GenWarp& w) {
         }
       }
     }
-    unsigned bal = __ballot_sync(0xffffffffu, ok);
     if (last) {
-      unsigned rows = bal;
+      // Venn rows: a lane builds its own when its lists are short, the warp
+      // builds the long ones together, one match at a time
+      auto vert = [&](int i) { return i == L + 1 ? x : w.stack[i]; };
+      const bool alone = ok && venn_walk_len(g, p, vert) <= p.lane_venn_max;
+      if (alone) venn_exclusive<1>(g, p, vert, w.venn[lane]);
+      unsigned rows = __ballot_sync(0xffffffffu, ok && !alone);
       while (rows) {
         const int who = __ffs(rows) - 1;
         rows &= rows - 1;
         const int xx = __shfl_sync(0xffffffffu, x, who);
-        if (lane == 0) w.stack[L + 1] = xx;
-        __syncwarp();
-        venn_general(g, p, w.stack, w.venn[who]);
+        auto vw = [&](int i) { return i == L + 1 ? xx : w.stack[i]; };
+        venn_exclusive<32>(g, p, vw, w.venn[who]);
       }
       __syncwarp();
-      if (ok) {
-        if constexpr (std::is_same<A, u64>::value)
-          credit(g, acc, p.exact ? placement_sum<u64>(p, w.venn[lane]) : placement_sum_reference(p, w.venn[lane]),
-                 w.stack[0]);
-        else
-          credit(g, acc, placement_sum<A>(p, w.venn[lane]), w.stack[0]);  // exact counts: exact placements
-      }
+      if (ok) credit(g, acc, placement_of<D, A>(p, w.venn[lane]), w.stack[0]);
       __syncwarp();
     } else {
+      unsigned bal = __ballot_sync(0xffffffffu, ok);
       while (bal) {
         const int who = __ffs(bal) - 1;
         bal &= bal - 1;
         const int xx = __shfl_sync(0xffffffffu, x, who);
         if (lane == 0) w.stack[L + 1] = xx;
         __syncwarp();
-        if constexpr (L < 4) acc += gen_level<L + 1, A>(g, p, w);
+        if constexpr (L < 4) acc += gen_level<L + 1, D, A>(g, p, w);
+        __syncwarp();
       }
     }
   }
   return acc;
 }
 
-// one warp per directed edge (u, v): u = core vertex A, v = core vertex B
-template <class A>
+// One warp per directed edge (u, v) at a time, u = core vertex A and v = core
+// vertex B (the reference's worklist of general_core_level0,
+// src/fringeCount.cu:567-663, with its degree pruning): warps take 32
+// consecutive list entries from a queue, find their owners in parallel and
+// then walk each entry's matches.  Work is spread per edge, so a hub's edges
+// go to many warps.
+template <int D, class A>
 __global__ void __launch_bounds__(kGenWarps * 32) general_core_kernel(GView g, const __grid_constant__ GenParams p,
-                                                                       int* __restrict__ queue, u64* __restrict__ slot) {
+                                                                       unsigned long long* __restrict__ queue,
+                                                                       u64* __restrict__ slot) {
   __shared__ GenWarp sw[kGenWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   GenWarp& w = sw[warp];
   A acc = A(0);
+  const unsigned long long m = (unsigned long long)g.m;
   for (;;) {
-    int u = 0;
-    if (lane == 0) u = atomicAdd(queue, 1);
-    u = __shfl_sync(0xffffffffu, u, 0);
-    if (u >= g.n) break;
-    const int du = g.deg[u];
-    if (du < p.startdeg) continue;
-    const long long ub = g.off[u];
-    for (int iv = 0; iv < du; iv++) {
-      const int v = __ldg(g.adj + ub + iv);
-      if (g.deg[v] < p.destdeg[0]) continue;  // init_wl_general
-      if (lane == 0) { w.stack[0] = u; w.stack[1] = v; }
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(queue, 32ULL);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= m) break;
+    const long long j = (long long)base + lane;
+    bool ok = j < (long long)m;
+    int u = 0, v = 0;
+    if (ok) {
+      int lo = 0, hi = g.n;  // owner: the last vertex with off[u] <= j
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (g.off[mid] <= j) lo = mid;
+        else hi = mid;
+      }
+      u = lo;
+      v = __ldg(g.adj + j);
+      ok = g.deg[u] >= p.startdeg && g.deg[v] >= p.destdeg[0];  // init_wl_general
+    }
+    unsigned bal = __ballot_sync(0xffffffffu, ok);
+    while (bal) {
+      const int who = __ffs(bal) - 1;
+      bal &= bal - 1;
+      const int uu = __shfl_sync(0xffffffffu, u, who), vv = __shfl_sync(0xffffffffu, v, who);
+      if (lane == 0) { w.stack[0] = uu; w.stack[1] = vv; }
       __syncwarp();
-      acc += gen_level<1, A>(g, p, w);
+      acc += gen_level<1, D, A>(g, p, w);
       __syncwarp();
     }
   }
@@ -1280,6 +1455,20 @@ void triangle_bitmap_geometry(const DevGraph& G, long long* per_block, int* bloc
 bool triangle_uses_bitmaps(const fsgc_matching_order&, const DevGraph& G, int mode) {
   const size_t smem = (size_t)3 * sizeof(int) * (size_t)std::max(1LL, G.max_outdeg);
   return mode == 0 && smem <= (size_t)96 * 1024 && G.m / 2 > 0;
+}
+
+// Bitmap kernel shared memory: the out-neighbour arrays (3 ints each), then as
+// long an N(a) stage as fits a 72 KB block (three blocks per SM): 4 bytes per
+// staged entry plus one row bit per warp.  Returns the stage length (a multiple
+// of 32, or 0) and the block's dynamic shared memory.
+int triangle_stage(int kmax, size_t* smem) {
+  const long long fixed = 3LL * 4 * std::max(1, kmax);
+  const long long budget = 72LL * 1024 - fixed - 16;
+  long long stage = budget > 0 ? budget / (4 + (kTriThreads / 32) * 4 / 32) : 0;
+  stage = std::min<long long>(stage, 8192) & ~31LL;
+  if (stage < 64) stage = 0;
+  *smem = (size_t)(4 * (stage + 4) + 4 * (stage / 32) * (kTriThreads / 32) + fixed);
+  return (int)stage;
 }
 
 }  // namespace
@@ -1500,7 +1689,8 @@ int enqueue_count_a(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& 
     tp.kmax = (int)G.max_outdeg;
     rotations3(f, false, tp.rot);
     if (me == 0) return FSGC_OK;
-    const size_t smem = (size_t)3 * sizeof(int) * (size_t)std::max(1, tp.kmax);
+    size_t smem = 0;
+    tp.stage = triangle_stage(tp.kmax, &smem);
     if (triangle_uses_bitmaps(mo, G, tp.mode)) {
       long long per_block;
       int blocks;
@@ -1512,8 +1702,14 @@ int enqueue_count_a(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& 
       cudaMemsetAsync(queue, 0, sizeof(int), s);
       if (smem > 48 * 1024)
         cudaFuncSetAttribute(triangle_bitmap_kernel<A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      triangle_bitmap_kernel<A><<<blocks, 256, smem, s>>>(gv, tp, queue, reinterpret_cast<unsigned*>(work.tri.ptr),
-                                                        per_block, job.d_slot);
+      triangle_bitmap_kernel<A><<<blocks, kTriThreads, smem, s>>>(
+          gv, tp, queue, reinterpret_cast<unsigned*>(work.tri.ptr), per_block,
+          reinterpret_cast<unsigned long long*>(work.small + kErrWord), job.d_slot);
+      *launches += 1;
+      // the kernel's error bits (a bulk copy that never completed) for the caller
+      if (work.h_err)
+        cudaMemcpyAsync(work.h_err, work.small + kErrWord, sizeof(u64), cudaMemcpyDeviceToHost, s);
+      return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
     } else {
       triangle_core_kernel<A><<<grid_for(me, TPB, 8), TPB, 0, s>>>(gv, tp, job.d_slot);
     }
@@ -1552,10 +1748,15 @@ int enqueue_count_a(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& 
     }
   }
   gp->nslots = ns;
-  int* queue = reinterpret_cast<int*>(work.small + 5);
-  cudaMemsetAsync(queue, 0, sizeof(int), s);
+  gp->lane_venn_max = kGenLaneVennMax;
+  auto* queue = reinterpret_cast<unsigned long long*>(work.small + 5);
+  cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
   const int blocks = sm_count() * 8;
-  general_core_kernel<A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
+  // the placement walk's state is sized by the step count
+  if (ns <= 32) general_core_kernel<32, A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
+  else if (ns <= 64) general_core_kernel<64, A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
+  else if (ns <= 128) general_core_kernel<128, A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
+  else general_core_kernel<kMaxSlots, A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
   *launches += 1;
   delete gp;
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;

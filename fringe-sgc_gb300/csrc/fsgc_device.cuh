@@ -103,6 +103,45 @@ __device__ __forceinline__ int lower_bound_dev(const int* __restrict__ a, int le
 }
 
 // ----------------------------------------------------------------------------
+// Bulk copies from global to shared memory (cp.async.bulk, the Blackwell copy
+// engine without a tensor map), completed on an mbarrier.  Source and
+// destination must be 16-byte aligned and the size a multiple of 16; the
+// copies used here read this GPU's own memory and are never multicast.
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Orders this thread's earlier shared-memory accesses before later copies.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// One thread: arm the barrier for `bytes` and start the copy.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Waits for the barrier's phase `parity` to complete, polling at most `limit`
+// times; false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity, int limit) {
+  for (int i = 0; i < limit; i++) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// ----------------------------------------------------------------------------
 // Exact counts: unsigned 128-bit values that saturate at 2^128 - 1 (every bit
 // set) instead of wrapping.  A product with a zero factor is zero; any other
 // operation with a saturated operand, or whose true result is >= 2^128 - 1,

@@ -89,9 +89,16 @@ struct Scratch {
 // queues, loader results) and a growable scratch arena (triangle-core bitmaps,
 // wedge-core hub cursors).
 struct DevWork {
-  u64* small = nullptr;  // 32 u64
+  u64* small = nullptr;  // 32 u64; small[kErrWord] collects kernel error bits
   Scratch tri;
+  u64* h_err = nullptr;  // pinned host copy of small[kErrWord], refreshed after kernels that can set it
 };
+constexpr int kErrWord = 10;
+
+// FSGC_ETIMEDOUT when a kernel of this work area gave up a bounded wait since
+// the last call (its count is void), FSGC_OK otherwise; clears the bits.
+// Call after the stream has been synchronised.
+int take_kernel_error(DevWork& w, cudaStream_t s);
 
 struct Launcher;  // forward
 

@@ -52,15 +52,63 @@ def test_default_line_has_the_contract_fields(monkeypatch, capsys):
     assert c["exact_counts"][names[0]]["exact"] == "7"
 
 
+def _fake_refrun(monkeypatch, ms_per_pattern, available=True):
+    import refrun
+    calls = []
+    monkeypatch.setattr(refrun, "available", lambda: available)
+
+    def write(path, *a):
+        with open(path, "wb") as f:
+            f.write((1024).to_bytes(4, "little") + (20000).to_bytes(4, "little"))
+    monkeypatch.setattr(refrun, "write_rmat_egr", write)
+
+    def run(egr, paths, timeout=None):
+        calls.append(paths[0])
+        return [{"core": 3, "aut": 2, "raw": 10, "count": 5, "ms": ms_per_pattern}]
+    monkeypatch.setattr(refrun, "run", run)
+    return calls
+
+
 def test_reference_arm_line(monkeypatch, capsys):
-    g = fsgc.gen_rmat(8, 4, seed=1)
-    monkeypatch.setattr(bench, "workload_graph", lambda scale=None: (g, 0.0))
-    monkeypatch.setattr(bench, "cpu_sample", lambda g, mos, budget, threads: (80.0, {"x": 1}))
+    """The reference arm's line: the reference's kernels' times (faked here),
+    full passes repeated within the budget, the first ones untimed."""
+    calls = _fake_refrun(monkeypatch, 250.0)
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "2", "--warmup", "3"])
     bench.main()
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unit"] == "patterns/s"
-    assert line["value"] == pytest.approx(8 / 80.0)
+    assert len(calls) == 8 * 5 and line["steps"] == 2 and line["warmup"] == 3
+    assert line["value"] == pytest.approx(8 / 2.0)  # 8 patterns x 250 ms per step
     assert line["e2e"] == {"value": line["value"], "unit": "patterns/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
-    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["cpu_baseline"]["kind"] == "reference" and line["config"]["value_bound"] is None
+    assert line["config"]["counts"]["edge_5_5"]["count"] == "5"
+
+
+def test_reference_arm_stops_within_its_budget(monkeypatch, capsys):
+    """Passes stop once the next would not end within the budget; one full pass
+    is then the timed step."""
+    import time as _time
+    clock = [1000.0]
+    monkeypatch.setattr(bench.time, "time", lambda: clock[0])
+    import refrun
+
+    def run(egr, paths, timeout=None):
+        clock[0] += 60.0
+        return [{"core": 3, "aut": 1, "raw": 1, "count": 1, "ms": 60000.0}]
+    _fake_refrun(monkeypatch, 0.0)
+    monkeypatch.setattr(refrun, "run", run)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "20", "--warmup", "5",
+                                      "--ref-budget", "700"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["steps"] == 1 and line["warmup"] == 0 and line["value"] == pytest.approx(8 / 480.0)
+    assert _time is not None
+
+
+def test_reference_arm_unavailable_without_the_cubin(monkeypatch, capsys):
+    _fake_refrun(monkeypatch, 1.0, available=False)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and "unavailable" in line

@@ -246,3 +246,37 @@ def test_cli_drop_in(tmp_path):
     cnt = int(re.search(r"(-?\d+) occurrences", r.stdout).group(1))
     o = oracle.count(g.nindex, g.nlist, (tmp_path / "motif.mo").read_bytes())
     assert cnt % (1 << 64) == o["count"]
+
+
+GENERAL_HUB = {
+    "5cycle": EXTRA["5cycle"],
+    "5cycle_chord_fringe": EXTRA["5cycle_chord_fringe"],
+    "4cycle_3": (7, [(0, 1), (1, 2), (2, 3), (3, 0), (0, 4), (1, 4), (2, 5), (3, 6), (0, 6)]),
+    "diamond_2": (6, [(0, 1), (1, 2), (2, 3), (3, 0), (0, 2), (1, 4), (3, 4), (0, 5), (1, 5), (2, 5)]),
+    "4path_ends": (6, [(0, 1), (1, 2), (2, 3), (0, 4), (3, 4), (1, 5)]),
+    "6cycle": (6, [(0, 1), (1, 2), (2, 3), (3, 4), (4, 5), (5, 0)]),
+}
+
+
+@pytest.mark.parametrize("hub_id", [0, 1199])
+def test_general_cores_on_hub_graph(ctx, hub_id):
+    """General cores (4-5 core vertices, few anchor sets) on a graph whose hub
+    has degree 600: the hub's list is the longest anchor list of many matches,
+    the one the Venn rows never walk, and it sends warps into long candidate
+    loops."""
+    rng = np.random.default_rng(11)
+    leaves = [x for x in range(1200) if x != hub_id][:600]
+    pairs = [(hub_id, i) for i in leaves]
+    pairs += list(zip(rng.integers(0, 1200, 2400).tolist(), rng.integers(0, 1200, 2400).tolist()))
+    g = fsgc.csr_from_edges(1200, pairs)
+    assert g.degrees().max() >= 600
+    gid = ctx.upload(g)
+    try:
+        pats = [(name, fsgc.preprocess(n, e)) for name, (n, e) in GENERAL_HUB.items()]
+        pats += [(c["name"], fsgc.MatchingOrder.from_bytes(bytes.fromhex(c["mo"]))) for c in RANDOM
+                 if bytes.fromhex(c["mo"])[0] >= 4 and bytes.fromhex(c["mo"])[1] <= 3][:12]
+        assert sum(mo.nodes >= 4 for _, mo in pats) >= 12
+        for name, mo in pats:
+            check(ctx, g, gid, name, mo)
+    finally:
+        ctx.release(gid)

@@ -98,10 +98,12 @@ def test_counts_match_reference_kernels(ctx, gname, tmp_path):
         ctx.release(gid)
 
 
-def test_bench_patterns_rmat16_match_reference_kernels(ctx, tmp_path):
-    """The eight RMAT workload patterns at scale 16 (n = 65,536, hubs of degree
-    up to ~9,700): fsgc and the reference's kernels agree bit for bit."""
-    g = fsgc.gen_rmat(16, 16, 0.57, 0.19, 0.19, 20251203)
+@pytest.mark.parametrize("scale", [16, 18])
+def test_bench_patterns_match_reference_kernels(ctx, tmp_path, scale):
+    """The eight RMAT workload patterns at scales 16 and 18 (n = 65,536 and
+    262,144, hubs of degree ~9,700 and ~25,000): fsgc and the reference's
+    kernels, run here, agree bit for bit."""
+    g = fsgc.gen_rmat(scale, 16, 0.57, 0.19, 0.19, 20251203)
     egr = str(tmp_path / "g.egr")
     fsgc.egr_write(egr, g)
     names = ["wedge_1_on_centre", "wedge_2_on_centre", "wedge_4_on_centre", "wedge_1_on_each_end",
@@ -122,3 +124,4 @@ def test_bench_patterns_rmat16_match_reference_kernels(ctx, tmp_path):
                    (r["count"], r["raw"], r["aut"], r["core"]), name
     finally:
         ctx.release(gid)
+
