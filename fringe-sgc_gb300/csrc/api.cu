@@ -41,6 +41,16 @@ struct fsgc_ctx {
   int member_cap = 0;
   void* flush_buf = nullptr;
   size_t flush_bytes = 0;
+  uint64_t slot_gen = 0;  // bumped whenever d_slots changes
+  // captured launch sequences of pattern sets, by (graph, matching orders)
+  struct SetGraph {
+    int gid;
+    uint64_t slot_gen, arena_gen;
+    cudaGraphExec_t exec;
+    std::vector<fsgc::CountJob> plan;  // host-side results of planning (core types, host values)
+  };
+  std::map<std::string, SetGraph> set_graphs;
+  std::map<std::string, int> set_seen;
 };
 
 struct fsgc_lane {
@@ -116,6 +126,7 @@ int ensure_slots(fsgc_ctx* c, int n) {
   CK(cudaMalloc((void**)&c->d_slots, sizeof(u64) * (size_t)cap), "slot allocation");
   CK(cudaMallocHost((void**)&c->h_slots, sizeof(u64) * (size_t)cap), "slot allocation");
   c->slot_cap = cap;
+  c->slot_gen++;
   return FSGC_OK;
 }
 
@@ -338,6 +349,19 @@ int count_tasks(fsgc_ctx* c, const fsgc_task* tasks, int nt, fsgc_result* res) {
   return FSGC_OK;
 }
 
+// Captured pattern-set launches of graph `gid` (all graphs when gid < 0).
+void drop_set_graphs(fsgc_ctx* c, int gid) {
+  for (auto it = c->set_graphs.begin(); it != c->set_graphs.end();) {
+    if (gid < 0 || it->second.gid == gid) {
+      cudaGraphExecDestroy(it->second.exec);
+      it = c->set_graphs.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  if (gid < 0) c->set_seen.clear();
+}
+
 }  // namespace
 
 namespace fsgc {
@@ -431,6 +455,7 @@ void fsgc_ctx_destroy(fsgc_ctx* c) {
   for (auto e : c->events) cudaEventDestroy(e);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
+  drop_set_graphs(c, -1);
   cudaFree(c->flush_buf);
   cudaFree(c->work.small);
   cudaFreeHost(c->work.h_err);
@@ -557,6 +582,7 @@ int fsgc_graph_release(fsgc_ctx* c, int gid) {
   auto it = c->graphs.find(gid);
   if (it == c->graphs.end()) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", gid);
   cudaStreamSynchronize(c->stream);
+  drop_set_graphs(c, gid);
   free_graph(it->second);
   c->graphs.erase(it);
   return FSGC_OK;
@@ -794,6 +820,113 @@ int fsgc_count_batch(fsgc_ctx* c, const fsgc_task* tasks, int ntasks, fsgc_resul
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   return count_tasks(c, tasks, ntasks, results);
+}
+
+// Many patterns on one graph in shared passes.  The first call with a given
+// (graph, matching orders) runs the launches directly and builds whatever the
+// graph still lacks; the second captures the launch sequence into a CUDA
+// graph; later calls replay it (one launch of the whole set) while the slot
+// array and the work arena stay where they were at capture.
+int fsgc_count_set(fsgc_ctx* c, int gid, const fsgc_matching_order* mos, int n, fsgc_result* results) {
+  if (!c || n < 0 || (n > 0 && (!mos || !results))) return fail(c, FSGC_EINVAL, "bad pattern-set arguments");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  if (n == 0) return FSGC_OK;
+  DevGraph* g = find_graph(c, gid);
+  if (!g) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", gid);
+  if (g->ngraphs > 0) return fail(c, FSGC_EINVAL, "graph %d is packed; use fsgc_count_packed", gid);
+  std::vector<fsgc_task> tasks((size_t)n);
+  for (int t = 0; t < n; t++) {
+    tasks[t].gid = gid;
+    tasks[t].mo = mos[t];
+    memset(&results[t], 0, sizeof(fsgc_result));
+  }
+  std::vector<u64> aut;
+  int st = plan_tasks(c, tasks.data(), n, aut);
+  if (st != FSGC_OK) return st;
+  st = ensure_slots(c, n);
+  if (st != FSGC_OK) return st;
+  st = ensure_events(c, 2);
+  if (st != FSGC_OK) return st;
+  std::vector<fsgc::CountJob> jobs((size_t)n);
+  std::vector<fsgc::CountJob*> run;
+  for (int t = 0; t < n; t++) {
+    jobs[t] = fsgc::CountJob{&tasks[t].mo, g, c->d_slots + t, 0, 0, false, c->exact_placements, nullptr, 1};
+    if (pattern_too_large(tasks[t].mo, *g)) {
+      jobs[t].host_only = true;
+      jobs[t].core_type = (tasks[t].mo.nodes == 3)
+                              ? ((__builtin_popcount(tasks[t].mo.list[1]) == 1) ? FSGC_CORE_WEDGE : FSGC_CORE_TRIANGLE)
+                              : FSGC_CORE_GENERAL;
+      results[t].flags |= FSGC_FLAG_PATTERN_TOO_LARGE;
+    } else {
+      run.push_back(&jobs[t]);
+    }
+  }
+  std::string key(reinterpret_cast<const char*>(&gid), sizeof(gid));
+  key.append(reinterpret_cast<const char*>(mos), sizeof(fsgc_matching_order) * (size_t)n);
+  key.push_back(c->exact_placements ? 'x' : 'r');
+  CK(cudaMemsetAsync(c->d_slots, 0, sizeof(u64) * (size_t)n, c->stream), "slot reset");
+  CK(cudaEventRecord(c->events[0], c->stream), "event");
+  auto it = c->set_graphs.find(key);
+  if (it != c->set_graphs.end() &&
+      (it->second.slot_gen != c->slot_gen || it->second.arena_gen != c->work.tri.gen)) {
+    cudaGraphExecDestroy(it->second.exec);
+    c->set_graphs.erase(it);
+    it = c->set_graphs.end();
+  }
+  if (it != c->set_graphs.end()) {
+    // the plan's host-side fields (core types, host values) as at capture
+    for (int t = 0; t < n; t++) {
+      if (jobs[t].host_only) continue;  // too large for the graph: decided above
+      jobs[t].core_type = it->second.plan[t].core_type;
+      jobs[t].host_only = it->second.plan[t].host_only;
+      jobs[t].host_value = it->second.plan[t].host_value;
+    }
+    CK(cudaGraphLaunch(it->second.exec, c->stream), "pattern-set replay");
+    c->launches += 1;
+  } else if (c->set_seen[key]++ > 0) {
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture");
+    uint64_t launches = 0;
+    st = fsgc::enqueue_count_set(run, c->stream, &launches, c->work);
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+    if (st != FSGC_OK || ce != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return fail(c, st != FSGC_OK ? st : FSGC_ECUDA, "capturing the pattern set failed");
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return cuda_fail(c, ie, "instantiating the pattern set");
+    c->set_graphs[key] = fsgc_ctx::SetGraph{gid, c->slot_gen, c->work.tri.gen, exec, jobs};
+    CK(cudaGraphLaunch(exec, c->stream), "pattern-set launch");
+    c->launches += launches;
+  } else {
+    st = fsgc::enqueue_count_set(run, c->stream, &c->launches, c->work);
+    if (st != FSGC_OK) {
+      cudaStreamSynchronize(c->stream);
+      return fail(c, st, "pattern-set count failed (%s)", cudaGetErrorString(cudaGetLastError()));
+    }
+  }
+  CK(cudaEventRecord(c->events[1], c->stream), "event");
+  CK(cudaMemcpyAsync(c->h_slots, c->d_slots, sizeof(u64) * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "readback");
+  CK(cudaStreamSynchronize(c->stream), "pattern-set count");
+  st = fsgc::take_kernel_error(c->work, c->stream);
+  if (st != FSGC_OK) return fail(c, st, "a counting kernel gave up a bounded wait; the counts are void");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->events[0], c->events[1]);
+  for (int t = 0; t < n; t++) {
+    fsgc_result& r = results[t];
+    const bool too_large = (r.flags & FSGC_FLAG_PATTERN_TOO_LARGE) != 0;
+    const u64 raw = jobs[t].host_only ? jobs[t].host_value : c->h_slots[t];
+    r.raw_total = too_large ? 0 : raw;
+    r.automorphisms = too_large ? 0 : aut[t];
+    r.count = too_large ? 0 : raw / aut[t];
+    r.core_type = jobs[t].core_type;
+    r.device_ms = ms / n;
+  }
+  return FSGC_OK;
 }
 
 // ---- lanes: asynchronous counts on their own streams.  The context lock is

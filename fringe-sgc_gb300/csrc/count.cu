@@ -175,6 +175,7 @@ struct EdgeParams {
   int f_u, f_uv, f_v, lim1, lim2;
 };
 
+
 template <class A>
 __global__ void edge_kernel(GView g, EdgeParams p, u64* __restrict__ slot) {
   const long long me = g.m / 2;
@@ -207,6 +208,69 @@ __global__ void packed_vertex_sum_kernel(GView g, const u64* __restrict__ vals, 
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x)
     credit(g, acc, vals[v], v);
   block_sum_to(acc, slot);
+}
+
+// Vertex- and edge-pass patterns counted together: one pass over the vertices
+// (stars, tailed triangles) or the oriented edges (edge-core formulas) adds
+// every pattern of the set into its own slot; each term is the single-pattern
+// kernel's.  Ordinary graphs and u64 counts only.
+constexpr int kPassFuse = 8;
+struct VertexSet {
+  int np;
+  int tailed[kPassFuse];  // 0: star, sum C(deg v, t); 1: tailed triangle, triangles(v) * C(deg v - 2, t)
+  int t[kPassFuse];
+  u64* slot[kPassFuse];
+};
+
+__global__ void vertex_set_kernel(GView g, const u64* __restrict__ vtri2, VertexSet p) {
+  u64 acc[kPassFuse];
+#pragma unroll
+  for (int q = 0; q < kPassFuse; q++) acc[q] = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < g.n; v += gridDim.x * blockDim.x) {
+    const int d = g.deg[v];
+    const u64 t2 = vtri2 ? vtri2[v] : 0;
+#pragma unroll
+    for (int q = 0; q < kPassFuse; q++) {
+      if (q >= p.np) break;
+      if (p.tailed[q]) {
+        if (t2) acc[q] += (t2 >> 1) * nck(d - 2, p.t[q]);
+      } else if (d >= p.t[q]) {
+        acc[q] += nck(d, p.t[q]);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kPassFuse; q++)
+    if (q < p.np) block_sum_to(acc[q], p.slot[q]);
+}
+
+struct EdgeSet {
+  int np;
+  EdgeParams e[kPassFuse];
+  u64* slot[kPassFuse];
+};
+
+__global__ void edge_set_kernel(GView g, EdgeSet p) {
+  const long long me = g.m / 2;
+  u64 acc[kPassFuse];
+#pragma unroll
+  for (int q = 0; q < kPassFuse; q++) acc[q] = 0;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < me; j += (long long)gridDim.x * blockDim.x) {
+    const int a = g.osrc[j], b = g.oadj[j];
+    const int u = max(a, b), v = min(a, b);  // the reference orients by id, v < u
+    const int du = g.deg[u], dv = g.deg[v];
+    const int sup = (int)g.osup[j];
+#pragma unroll
+    for (int q = 0; q < kPassFuse; q++) {
+      if (q >= p.np) break;
+      const EdgeParams& e = p.e[q];
+      if (du > e.lim1 && dv > e.lim1 && du + dv > e.lim2)  // init_wl_edge pruning
+        acc[q] += edge_formula<u64>(du, dv, sup, e.f_u, e.f_uv, e.f_v);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kPassFuse; q++)
+    if (q < p.np) block_sum_to(acc[q], p.slot[q]);
 }
 
 // ------------------------------------------------------------- triangle core
@@ -386,12 +450,23 @@ constexpr int kTriWalkRatio = 16;
 constexpr int kTriThreads = 256;
 constexpr int kBulkWaitPolls = 1 << 22;  // bounded wait for a bulk copy
 
-template <class A>
-__global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g, TriParams p, int* __restrict__ queue,
+// Triangle-core patterns counted together: the bitmaps, roles and Venn sizes
+// of a triangle do not depend on the pattern, only the pruning thresholds and
+// the placement formulas do.  p.sum1 (the vertex gate) is the set's smallest.
+constexpr int kTriFuse = 4;
+struct TriSet {
+  int np;
+  int sum1[kTriFuse], sum2[kTriFuse], sum3[kTriFuse];
+  Rot3 rot[kTriFuse];
+  u64* slot[kTriFuse];
+};
+
+template <int NP, class A>
+__global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g, TriParams p, TriSet ts,
+                                                                      int* __restrict__ queue,
                                                                       unsigned* __restrict__ bits_all,
                                                                       long long bits_per_block,
-                                                                      unsigned long long* __restrict__ err,
-                                                                      u64* __restrict__ slot) {
+                                                                      unsigned long long* __restrict__ err) {
   extern __shared__ __align__(16) int s_dyn[];
   __shared__ int s_a;
   __shared__ __align__(8) unsigned long long s_bar;
@@ -406,7 +481,9 @@ __global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g
   unsigned parity = 0;
   if (threadIdx.x == 0 && stage > 0) mbar_init(&s_bar, 1);
   __syncthreads();
-  A acc = A(0);
+  A acc[NP];
+#pragma unroll
+  for (int q = 0; q < NP; q++) acc[q] = A(0);
   for (;;) {
     if (threadIdx.x == 0) s_a = atomicAdd(queue, 1);
     __syncthreads();
@@ -520,9 +597,6 @@ __global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g
           };
           const int iu = ord[0], iv = ord[1], iw = ord[2];
           const int du = dx[iu], dv = dx[iv], dw = dx[iw];
-          const int th1 = max(p.sum1, p.sum2 - du);
-          const int th2 = max(max(p.sum1, p.sum3 - du - dv), max(p.sum2 - du, p.sum2 - dv));
-          if (!((du >= p.sum1) && (dv >= th1) && (dw >= th2))) continue;
           const int p12 = sup(iu, iv), t13 = sup(iu, iw), t23 = sup(iv, iw);
           const int c12 = p12 - (c123 + 1), c13 = t13 - (c123 + 1), c23 = t23 - (c123 + 1);
           int venn[8];
@@ -531,15 +605,25 @@ __global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g
           venn[IV] = dv - (c12 + c23 + (c123 + 2));
           venn[IW] = dw - (c13 + c23 + (c123 + 2));
           venn[IUV] = c12; venn[IUW] = c13; venn[IVW] = c23; venn[IUVW] = c123;
-          A t = A(0);
-          for (int r = 0; r < p.rot.count; r++) t += fc3<A>(p.rot.fr[r], venn);
-          credit(g, acc, t, a);
+#pragma unroll
+          for (int q = 0; q < NP; q++) {
+            if (q >= ts.np) break;
+            // the reference's pruning (init_wl_triangle, common3_triangle)
+            const int th1 = max(ts.sum1[q], ts.sum2[q] - du);
+            const int th2 = max(max(ts.sum1[q], ts.sum3[q] - du - dv), max(ts.sum2[q] - du, ts.sum2[q] - dv));
+            if (!((du >= ts.sum1[q]) && (dv >= th1) && (dw >= th2))) continue;
+            A t = A(0);
+            for (int r = 0; r < ts.rot[q].count; r++) t += fc3<A>(ts.rot[q].fr[r], venn);
+            credit(g, acc[q], t, a);
+          }
         }
       }
     }
     __syncthreads();
   }
-  block_sum_to(acc, slot);
+#pragma unroll
+  for (int q = 0; q < NP; q++)
+    if (q < ts.np) block_sum_to(acc[q], ts.slot[q]);
 }
 
 // ------------------------------------------------------------- wedge core
@@ -685,20 +769,35 @@ __device__ void block_scan_inplace(int* x, int n, WedgeSmem<BIG>& S) {
   if (tid == 0) x[n] = carry;
 }
 
-template <bool BIG, class A>
-__device__ __forceinline__ void eval_pair(const GView& g, const WedgeParams& p, WedgeSmem<BIG>& S, int lo, int o,
-                                          unsigned C, int dw, int v, int dv, int thres, A& acc) {
-  if (dw >= thres) {
-    const bool vw = (S.adjbits[o >> 5] >> (o & 31)) & 1u;
-    credit(g, acc, A((u64)C) * wedge_formula<A>(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1), v);
+// Patterns of this core shape counted together: the centre counts C(v, w)
+// do not depend on the pattern, so one counting pass serves every pattern of
+// the set and each pair is evaluated once per pattern.  lim is the smallest
+// endpoint degree any of them takes.
+constexpr int kWedgeFuse = 4;
+struct WedgeSet {
+  int np;
+  int lim;
+  WedgeParams w[kWedgeFuse];
+  u64* slot[kWedgeFuse];
+};
+
+template <bool BIG, int NP, class A>
+__device__ __forceinline__ void eval_pair(const GView& g, const WedgeSet& ws, WedgeSmem<BIG>& S, int o, unsigned C,
+                                          int dw, int v, int dv, A* acc) {
+  const bool vw = (S.adjbits[o >> 5] >> (o & 31)) & 1u;
+#pragma unroll
+  for (int q = 0; q < NP; q++) {
+    if (q >= ws.np) break;
+    const WedgeParams& p = ws.w[q];
+    if (dv >= p.lim && dw >= max(p.lim, p.minsum - dv))
+      credit(g, acc[q], A((u64)C) * wedge_formula<A>(dv, dw, vw, p.f_v, p.f_vw, p.f_w, (int)C - 1), v);
   }
 }
 
-template <bool BIG, class A>
-__global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, WedgeParams p, int* __restrict__ queue,
+template <bool BIG, int NP, class A>
+__global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, WedgeSet ws, int* __restrict__ queue,
                                                                    long long* __restrict__ gcur, int* __restrict__ gpre,
-                                                                   long long gstride, ChunkTable tab,
-                                                                   u64* __restrict__ slot) {
+                                                                   long long gstride, ChunkTable tab) {
   constexpr int WORDS = WedgeCfg<BIG>::WORDS;
   constexpr int TW = WedgeCfg<BIG>::TW;
   extern __shared__ unsigned char s_raw[];
@@ -710,7 +809,9 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
   for (int i = tid; i < WORDS; i += blockDim.x) S.cnt[i] = 0;
   for (int i = tid; i < TW; i += blockDim.x) S.touched[i] = 0;
   for (int i = tid; i < WedgeCfg<BIG>::CH_MAX / 32; i += blockDim.x) S.adjbits[i] = 0;
-  A acc = A(0);
+  A acc[NP];
+#pragma unroll
+  for (int q = 0; q < NP; q++) acc[q] = A(0);
   for (;;) {
     if (tid == 0) {
       S.v = atomicAdd(queue, 1);
@@ -720,11 +821,10 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
     const int v = S.v;
     if (v >= g.n) break;
     const int dv = g.deg[v];
-    if (dv < p.lim || (BIG ? dv <= kWDvMax : dv > kWDvMax)) {
+    if (dv < ws.lim || (BIG ? dv <= kWDvMax : dv > kWDvMax)) {
       __syncthreads();
       continue;
     }
-    const int thres = max(p.lim, p.minsum - dv);
     // counter layout: `bits` per counter, 2^lper counters per word, CH ids per chunk
     const int bits = BIG ? 32 : wedge_counter_bits(dv);
     const int lper = BIG ? 0 : (bits == 16 ? 1 : (bits == 8 ? 2 : 3));
@@ -861,7 +961,7 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
               const int kbit = nth_set_bit(nzS, i - exS);  // low bit of the counter
               const unsigned C = (wordS >> kbit) & cmask;
               const int o = (wdS << lper) + (kbit >> lbits);
-              eval_pair<BIG, A>(g, p, S, lo, o, C, g.deg[lo + o], v, dv, thres, acc);
+              eval_pair<BIG, NP, A>(g, ws, S, o, C, g.deg[lo + o], v, dv, acc);
             }
           }
         }
@@ -886,7 +986,9 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
       __syncthreads();
     }
   }
-  block_sum_to(acc, slot);
+#pragma unroll
+  for (int q = 0; q < NP; q++)
+    if (q < ws.np) block_sum_to(acc[q], ws.slot[q]);
 }
 
 // boundary table: pass 1 gives each vertex of degree >= min_deg a row
@@ -1439,6 +1541,7 @@ int ensure_plain_scratch(Scratch& sc, size_t need, cudaStream_t s) {
     return FSGC_ENOMEM;
   }
   sc.bytes = need;
+  sc.gen++;
   return FSGC_OK;
 }
 
@@ -1548,6 +1651,68 @@ int prepare_for_count(const fsgc_matching_order& mo, DevGraph& G, cudaStream_t s
 }
 
 namespace {
+// Both pair kernels of the fringe-free-centre wedge core for a set of
+// patterns: endpoints of degree <= kWDvMax, then hub endpoints (cursors and
+// segment offsets in the work arena).
+template <int NP, class A>
+int launch_wedge_set(DevGraph& G, const GView& gv, const WedgeSet& ws, cudaStream_t s, uint64_t* launches,
+                     DevWork& work) {
+  int* q1 = reinterpret_cast<int*>(work.small + 7);
+  int* q2 = reinterpret_cast<int*>(work.small + 8);
+  int st = ensure_chunk_table(G, s, launches, work.small + 9);
+  if (st != FSGC_OK) return st;
+  const ChunkTable tab{G.ctab_id, G.ctab_pos, G.ctab_K};
+  cudaMemsetAsync(q1, 0, 2 * sizeof(u64), s);
+  const int blocks = sm_count();
+  {
+    const size_t smem = sizeof(WedgeSmem<false>);
+    cudaFuncSetAttribute(wedge_chunk_kernel<false, NP, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    wedge_chunk_kernel<false, NP, A><<<blocks, kWThreads, smem, s>>>(gv, ws, q1, nullptr, nullptr, 0, tab);
+    *launches += 1;
+  }
+  if (G.maxdeg > kWDvMax) {
+    // hub endpoints: cursors (2 x int64) and segment offsets (int32) per block
+    const long long gs = G.maxdeg;
+    const size_t need = (size_t)blocks * ((size_t)2 * gs * sizeof(long long) + (size_t)(gs + 1) * sizeof(int));
+    st = ensure_plain_scratch(work.tri, std::max(need, work.tri.bytes), s);
+    if (st != FSGC_OK) return st;
+    long long* gcur = reinterpret_cast<long long*>(work.tri.ptr);
+    int* gpre = reinterpret_cast<int*>(gcur + (size_t)blocks * 2 * gs);
+    const size_t smem = sizeof(WedgeSmem<true>);
+    cudaFuncSetAttribute(wedge_chunk_kernel<true, NP, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    wedge_chunk_kernel<true, NP, A><<<blocks, kWThreads, smem, s>>>(gv, ws, q2, gcur, gpre, gs, tab);
+    *launches += 1;
+  }
+  return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+
+// The triangle bitmap kernel for a set of patterns (tp: shared fields, with
+// tp.sum1 the set's smallest vertex gate).
+template <int NP, class A>
+int launch_triangle_set(DevGraph& G, const GView& gv, TriParams tp, const TriSet& ts, cudaStream_t s,
+                        uint64_t* launches, DevWork& work) {
+  size_t smem = 0;
+  tp.kmax = (int)G.max_outdeg;
+  tp.stage = triangle_stage(tp.kmax, &smem);
+  long long per_block;
+  int blocks;
+  triangle_bitmap_geometry(G, &per_block, &blocks);
+  const size_t need = sizeof(unsigned) * (size_t)per_block * (size_t)blocks;
+  int st = ensure_plain_scratch(work.tri, need, s);
+  if (st != FSGC_OK) return st;
+  int* queue = reinterpret_cast<int*>(work.small + 6);
+  cudaMemsetAsync(queue, 0, sizeof(int), s);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(triangle_bitmap_kernel<NP, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  triangle_bitmap_kernel<NP, A><<<blocks, kTriThreads, smem, s>>>(
+      gv, tp, ts, queue, reinterpret_cast<unsigned*>(work.tri.ptr), per_block,
+      reinterpret_cast<unsigned long long*>(work.small + kErrWord));
+  *launches += 1;
+  // the kernel's error bits (a bulk copy that never completed) for the caller
+  if (work.h_err) cudaMemcpyAsync(work.h_err, work.small + kErrWord, sizeof(u64), cudaMemcpyDeviceToHost, s);
+  return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+
 template <class A>
 int enqueue_count_a(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work) {
   const fsgc_matching_order& mo = *job.mo;
@@ -1632,34 +1797,13 @@ int enqueue_count_a(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& 
     const int sum1 = std::min(std::min(min_u, min_v), min_w);
     const int lim = std::min(min_v, min_w);
     if (f[IUVW] == 0 && f[IUV] == 0 && f[IUW] == 0 && f[IU] == 0) {
-      WedgeParams wp{f[IV], f[IVW], f[IW], lim, min_v + min_w};
-      int* q1 = reinterpret_cast<int*>(work.small + 7);
-      int* q2 = reinterpret_cast<int*>(work.small + 8);
-      st = ensure_chunk_table(G, s, launches, work.small + 9);
-      if (st != FSGC_OK) return st;
-      const ChunkTable tab{G.ctab_id, G.ctab_pos, G.ctab_K};
-      cudaMemsetAsync(q1, 0, 2 * sizeof(u64), s);
-      const int blocks = sm_count();
-      {
-        const size_t smem = sizeof(WedgeSmem<false>);
-        cudaFuncSetAttribute(wedge_chunk_kernel<false, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        wedge_chunk_kernel<false, A><<<blocks, kWThreads, smem, s>>>(gv, wp, q1, nullptr, nullptr, 0, tab, job.d_slot);
-        *launches += 1;
-      }
-      if (G.maxdeg > kWDvMax) {
-        // hub endpoints: cursors (2 x int64) and segment offsets (int32) per block
-        const long long gs = G.maxdeg;
-        const size_t need = (size_t)blocks * ((size_t)2 * gs * sizeof(long long) + (size_t)(gs + 1) * sizeof(int));
-        st = ensure_plain_scratch(work.tri, std::max(need, work.tri.bytes), s);
-        if (st != FSGC_OK) return st;
-        long long* gcur = reinterpret_cast<long long*>(work.tri.ptr);
-        int* gpre = reinterpret_cast<int*>(gcur + (size_t)blocks * 2 * gs);
-        const size_t smem = sizeof(WedgeSmem<true>);
-        cudaFuncSetAttribute(wedge_chunk_kernel<true, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        wedge_chunk_kernel<true, A><<<blocks, kWThreads, smem, s>>>(gv, wp, q2, gcur, gpre, gs, tab, job.d_slot);
-        *launches += 1;
-      }
-      return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+      WedgeSet ws;
+      memset(&ws, 0, sizeof(ws));
+      ws.np = 1;
+      ws.lim = lim;
+      ws.w[0] = WedgeParams{f[IV], f[IVW], f[IW], lim, min_v + min_w};
+      ws.slot[0] = job.d_slot;
+      return launch_wedge_set<1, A>(G, gv, ws, s, launches, work);
     }
     GWedgeParams gp;
     gp.min_u = min_u; gp.lim = lim; gp.sum1 = sum1; gp.sum2 = sum2; gp.sum3 = sum3;
@@ -1689,27 +1833,14 @@ int enqueue_count_a(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& 
     tp.kmax = (int)G.max_outdeg;
     rotations3(f, false, tp.rot);
     if (me == 0) return FSGC_OK;
-    size_t smem = 0;
-    tp.stage = triangle_stage(tp.kmax, &smem);
     if (triangle_uses_bitmaps(mo, G, tp.mode)) {
-      long long per_block;
-      int blocks;
-      triangle_bitmap_geometry(G, &per_block, &blocks);
-      const size_t need = sizeof(unsigned) * (size_t)per_block * (size_t)blocks;
-      st = ensure_plain_scratch(work.tri, need, s);
-      if (st != FSGC_OK) return st;
-      int* queue = reinterpret_cast<int*>(work.small + 6);
-      cudaMemsetAsync(queue, 0, sizeof(int), s);
-      if (smem > 48 * 1024)
-        cudaFuncSetAttribute(triangle_bitmap_kernel<A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      triangle_bitmap_kernel<A><<<blocks, kTriThreads, smem, s>>>(
-          gv, tp, queue, reinterpret_cast<unsigned*>(work.tri.ptr), per_block,
-          reinterpret_cast<unsigned long long*>(work.small + kErrWord), job.d_slot);
-      *launches += 1;
-      // the kernel's error bits (a bulk copy that never completed) for the caller
-      if (work.h_err)
-        cudaMemcpyAsync(work.h_err, work.small + kErrWord, sizeof(u64), cudaMemcpyDeviceToHost, s);
-      return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+      TriSet ts;
+      memset(&ts, 0, sizeof(ts));
+      ts.np = 1;
+      ts.sum1[0] = tp.sum1; ts.sum2[0] = tp.sum2; ts.sum3[0] = tp.sum3;
+      ts.rot[0] = tp.rot;
+      ts.slot[0] = job.d_slot;
+      return launch_triangle_set<1, A>(G, gv, tp, ts, s, launches, work);
     } else {
       triangle_core_kernel<A><<<grid_for(me, TPB, 8), TPB, 0, s>>>(gv, tp, job.d_slot);
     }
@@ -1767,25 +1898,186 @@ int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& wo
   return job.exact_count ? enqueue_count_a<X128>(job, s, launches, work) : enqueue_count_a<u64>(job, s, launches, work);
 }
 
+// Many patterns on one graph: patterns whose kernels share their match
+// enumeration run as sets -- stars and tailed triangles in one vertex pass,
+// edge-core formulas in one pass over the oriented edges, fringe-free-centre
+// wedges over one set of centre counts, triangle cores over one set of
+// bitmaps -- and every other pattern as a count of its own.  Each job's
+// result goes to its own slot; the values equal the single-pattern kernels'.
+int enqueue_count_set(std::vector<CountJob*>& jobs, cudaStream_t s, uint64_t* launches, DevWork& work) {
+  if (jobs.empty()) return FSGC_OK;
+  DevGraph& G = *jobs[0]->g;
+  for (CountJob* j : jobs)
+    if (j->g != &G || j->exact_count || G.ngraphs > 0) return FSGC_EINVAL;
+  int st = prepare_graph(G, s, launches, work.small);
+  if (st != FSGC_OK) return st;
+  GView gv = G.view();
+  std::vector<std::pair<CountJob*, std::pair<int, int>>> verts;  // (job, (tailed, t))
+  std::vector<std::pair<CountJob*, EdgeParams>> edges;
+  std::vector<std::pair<CountJob*, WedgeParams>> wedges;
+  std::vector<std::pair<CountJob*, TriParams>> tris;
+  std::vector<CountJob*> single;
+  for (CountJob* jp : jobs) {
+    CountJob& job = *jp;
+    const fsgc_matching_order& mo = *job.mo;
+    job.host_only = false;
+    job.host_value = 0;
+    job.per_member_div = 1;
+    if (mo.nodes == 1 && mo.anchorsets > 0 && mo.fcnt[0] > 1) {
+      job.core_type = FSGC_CORE_VERTEX;
+      verts.push_back({jp, {0, (int)mo.fcnt[0]}});
+      continue;
+    }
+    if (mo.nodes == 2) {
+      int f[4] = {0, 0, 0, 0};
+      for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 3] = mo.fcnt[i];
+      const int f_u = std::min(f[1], f[2]), f_uv = f[3], f_v = std::max(f[1], f[2]);
+      job.core_type = FSGC_CORE_EDGE;
+      if (f_uv == 1 && (f_u == 0 || f_v == 0)) {
+        if (f_u == 0 && f_v == 0) { single.push_back(jp); continue; }  // the triangle total
+        verts.push_back({jp, {1, f_v}});
+      } else {
+        edges.push_back({jp, EdgeParams{f_u, f_uv, f_v, f_u + f_uv, f_u + f_uv + f_v}});
+      }
+      continue;
+    }
+    if (mo.nodes == 3) {
+      int f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (int i = 0; i < mo.anchorsets; i++) f[mo.anch[i] & 7] = mo.fcnt[i];
+      if (__builtin_popcount(mo.list[1]) == 1) {
+        if (mo.list[1] == 2) {
+          std::swap(f[IU], f[IV]);
+          std::swap(f[IUW], f[IVW]);
+        }
+        if (f[IUVW] == 0 && f[IUV] == 0 && f[IUW] == 0 && f[IU] == 0) {
+          const int min_v = f[IUVW] + f[IUV] + f[IVW] + f[IV] + 1;
+          const int min_w = f[IUVW] + f[IUW] + f[IVW] + f[IW] + 1;
+          job.core_type = FSGC_CORE_WEDGE;
+          wedges.push_back({jp, WedgeParams{f[IV], f[IVW], f[IW], std::min(min_v, min_w), min_v + min_w}});
+          continue;
+        }
+      } else {
+        const int min_u = f[IUVW] + f[IUV] + f[IUW] + f[IU];
+        const int min_v = f[IUVW] + f[IUV] + f[IVW] + f[IV];
+        const int min_w = f[IUVW] + f[IUW] + f[IVW] + f[IW];
+        const bool clique = (f[IUVW] == 1) && (f[IUV] + f[IUW] + f[IVW] == 0) &&
+                            ((f[IU] == 0) + (f[IV] == 0) + (f[IW] == 0) >= 2);
+        if (!clique && triangle_uses_bitmaps(mo, G, 0)) {
+          TriParams tp;
+          memset(&tp, 0, sizeof(tp));
+          tp.sum3 = min_u + min_v + min_w + 6;
+          tp.sum2 = tp.sum3 - (std::max(std::max(min_u, min_v), min_w) + 2);
+          tp.sum1 = std::min(std::min(min_u, min_v), min_w) + 2;
+          tp.relabel = G.tri_relabel ? 1 : 0;
+          rotations3(f, false, tp.rot);
+          job.core_type = FSGC_CORE_TRIANGLE;
+          tris.push_back({jp, tp});
+          continue;
+        }
+      }
+    }
+    single.push_back(jp);
+  }
+  const int TPB = kTPB;
+  for (size_t b = 0; b < verts.size(); b += kPassFuse) {
+    VertexSet vs;
+    memset(&vs, 0, sizeof(vs));
+    bool tailed = false;
+    for (size_t i = b; i < std::min(verts.size(), b + kPassFuse); i++) {
+      const int q = vs.np++;
+      vs.tailed[q] = verts[i].second.first;
+      vs.t[q] = verts[i].second.second;
+      vs.slot[q] = verts[i].first->d_slot;
+      tailed |= vs.tailed[q] != 0;
+    }
+    if (tailed) {
+      st = ensure_vertex_triangles(G, s, launches);
+      if (st != FSGC_OK) return st;
+    }
+    vertex_set_kernel<<<grid_for(G.n, TPB, 8), TPB, 0, s>>>(gv, tailed ? G.vtri2 : nullptr, vs);
+    *launches += 1;
+  }
+  for (size_t b = 0; b < edges.size(); b += kPassFuse) {
+    EdgeSet es;
+    memset(&es, 0, sizeof(es));
+    for (size_t i = b; i < std::min(edges.size(), b + kPassFuse); i++) {
+      const int q = es.np++;
+      es.e[q] = edges[i].second;
+      es.slot[q] = edges[i].first->d_slot;
+    }
+    if (G.m / 2 > 0) {
+      edge_set_kernel<<<grid_for(G.m / 2, TPB, 8), TPB, 0, s>>>(gv, es);
+      *launches += 1;
+    }
+  }
+  for (size_t b = 0; b < wedges.size(); b += kWedgeFuse) {
+    WedgeSet ws;
+    memset(&ws, 0, sizeof(ws));
+    ws.lim = 1 << 30;
+    for (size_t i = b; i < std::min(wedges.size(), b + kWedgeFuse); i++) {
+      const int q = ws.np++;
+      ws.w[q] = wedges[i].second;
+      ws.slot[q] = wedges[i].first->d_slot;
+      ws.lim = std::min(ws.lim, ws.w[q].lim);
+    }
+    st = ws.np == 1 ? launch_wedge_set<1, u64>(G, gv, ws, s, launches, work)
+                    : launch_wedge_set<kWedgeFuse, u64>(G, gv, ws, s, launches, work);
+    if (st != FSGC_OK) return st;
+  }
+  for (size_t b = 0; b < tris.size(); b += kTriFuse) {
+    TriSet ts;
+    memset(&ts, 0, sizeof(ts));
+    TriParams shared = tris[b].second;
+    for (size_t i = b; i < std::min(tris.size(), b + kTriFuse); i++) {
+      const int q = ts.np++;
+      const TriParams& tp = tris[i].second;
+      ts.sum1[q] = tp.sum1; ts.sum2[q] = tp.sum2; ts.sum3[q] = tp.sum3;
+      ts.rot[q] = tp.rot;
+      ts.slot[q] = tris[i].first->d_slot;
+      shared.sum1 = std::min(shared.sum1, tp.sum1);
+    }
+    st = ts.np == 1 ? launch_triangle_set<1, u64>(G, gv, shared, ts, s, launches, work)
+                    : launch_triangle_set<kTriFuse, u64>(G, gv, shared, ts, s, launches, work);
+    if (st != FSGC_OK) return st;
+  }
+  for (CountJob* jp : single) {
+    st = enqueue_count(*jp, s, launches, work);
+    if (st != FSGC_OK) return st;
+  }
+  return FSGC_OK;
+}
+
 // Launchers for callers that bring their own device memory (noalloc.cu): the
 // wedge-core pair kernels on a view whose deg[] the caller filled.
+namespace {
+WedgeSet single_wedge(int f_v, int f_vw, int f_w, int lim, int minsum, u64* slot) {
+  WedgeSet ws;
+  memset(&ws, 0, sizeof(ws));
+  ws.np = 1;
+  ws.lim = lim;
+  ws.w[0] = WedgeParams{f_v, f_vw, f_w, lim, minsum};
+  ws.slot[0] = slot;
+  return ws;
+}
+}  // namespace
+
 int launch_wedge_small(const GView& gv, int f_v, int f_vw, int f_w, int lim, int minsum, int* queue, u64* slot,
                        cudaStream_t s) {
-  WedgeParams wp{f_v, f_vw, f_w, lim, minsum};
+  const WedgeSet ws = single_wedge(f_v, f_vw, f_w, lim, minsum, slot);
   const size_t smem = sizeof(WedgeSmem<false>);
-  cudaFuncSetAttribute(wedge_chunk_kernel<false, u64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  wedge_chunk_kernel<false, u64><<<sm_count(), kWThreads, smem, s>>>(gv, wp, queue, nullptr, nullptr, 0,
-                                                                ChunkTable{nullptr, nullptr, 0}, slot);
+  cudaFuncSetAttribute(wedge_chunk_kernel<false, 1, u64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  wedge_chunk_kernel<false, 1, u64><<<sm_count(), kWThreads, smem, s>>>(gv, ws, queue, nullptr, nullptr, 0,
+                                                                   ChunkTable{nullptr, nullptr, 0});
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }
 
 int launch_wedge_big(const GView& gv, int f_v, int f_vw, int f_w, int lim, int minsum, int* queue, long long* gcur,
                      int* gpre, long long gstride, int blocks, u64* slot, cudaStream_t s) {
-  WedgeParams wp{f_v, f_vw, f_w, lim, minsum};
+  const WedgeSet ws = single_wedge(f_v, f_vw, f_w, lim, minsum, slot);
   const size_t smem = sizeof(WedgeSmem<true>);
-  cudaFuncSetAttribute(wedge_chunk_kernel<true, u64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  wedge_chunk_kernel<true, u64><<<blocks, kWThreads, smem, s>>>(gv, wp, queue, gcur, gpre, gstride,
-                                                           ChunkTable{nullptr, nullptr, 0}, slot);
+  cudaFuncSetAttribute(wedge_chunk_kernel<true, 1, u64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  wedge_chunk_kernel<true, 1, u64><<<blocks, kWThreads, smem, s>>>(gv, ws, queue, gcur, gpre, gstride,
+                                                              ChunkTable{nullptr, nullptr, 0});
   return cudaGetLastError() == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }
 

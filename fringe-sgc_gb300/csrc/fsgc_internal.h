@@ -83,6 +83,7 @@ struct Scratch {
   void* ptr = nullptr;
   size_t bytes = 0;
   int layout_n = -1, layout_rows = -1;
+  uint64_t gen = 0;  // bumped whenever ptr changes (captured launch sequences hold the pointer)
 };
 
 // Per-context device work areas: a few u64 counters/queues (kernel work
@@ -136,6 +137,9 @@ int wedge_small_max_degree();
 
 // Enqueue the kernels that add the raw total of `mo` on `g` into *d_slot.
 int enqueue_count(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& work);
+// Many jobs on one ordinary graph (u64 counts): patterns whose kernels share
+// their match enumeration are counted in shared passes (count.cu).
+int enqueue_count_set(std::vector<CountJob*>& jobs, cudaStream_t s, uint64_t* launches, DevWork& work);
 // Builds, on `s` and synchronously, every per-graph structure a count of `mo`
 // would otherwise build on first use, so that counts enqueued afterwards on
 // other streams only read the graph.

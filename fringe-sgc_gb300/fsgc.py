@@ -120,6 +120,8 @@ def lib():
             "fsgc_graph_info_get": (I, [P, I, C.POINTER(GraphInfo)]),
             "fsgc_count": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(Result)]),
             "fsgc_count_batch": (I, [P, C.POINTER(Task), I, C.POINTER(Result)]),
+            "fsgc_count_set": (I, [P, I, C.POINTER(MatchingOrder), I, C.POINTER(Result)]),
+            "fsgc_divisor_from_self_count": (I, [C.c_ulonglong, C.POINTER(C.c_ulonglong)]),
             "fsgc_count_exact": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(ExactResult)]),
             "fsgc_graph_from_packed_csr": (I, [P, I, I64, P, P, I, P, C.POINTER(C.c_int)]),
             "fsgc_count_packed": (I, [P, I, C.POINTER(MatchingOrder), C.POINTER(Result)]),
@@ -397,6 +399,15 @@ class Context:
             arr[i].mo = mo
         res = (Result * len(tasks))()
         _check(lib().fsgc_count_batch(self.ptr, arr, len(tasks), res), "count_batch", self.ptr)
+        return list(res)
+
+    def count_set(self, gid, mos):
+        """Many patterns on one graph in shared passes (fsgc_count_set); the
+        second call with the same patterns captures a CUDA graph, later calls
+        replay it."""
+        arr = (MatchingOrder * len(mos))(*mos)
+        res = (Result * len(mos))()
+        _check(lib().fsgc_count_set(self.ptr, gid, arr, len(mos), res), "count_set", self.ptr)
         return list(res)
 
 

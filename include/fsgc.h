@@ -199,6 +199,18 @@ typedef struct fsgc_exact_result {
 } fsgc_exact_result;
 int fsgc_count_exact(fsgc_ctx* ctx, int gid, const fsgc_matching_order* mo, fsgc_exact_result* out);
 
+/* Many patterns on one resident graph in one call (the batching-on-one-graph
+ * workload; the reference runs one fringeCount process per pattern).  Patterns
+ * whose kernels share their match enumeration are counted in shared passes:
+ * stars and tailed triangles in one pass over the vertices, edge-core
+ * formulas in one pass over the edges, fringe-free-centre wedge cores over
+ * one set of centre counts, triangle cores over one set of per-vertex
+ * bitmaps; the rest one by one.  Every result equals fsgc_count's.  The
+ * second call with the same graph and patterns captures the launches into a
+ * CUDA graph and later calls replay it.  device_ms is the whole set's device
+ * time divided by n.  Ordinary (not packed) graphs; u64 counts. */
+int fsgc_count_set(fsgc_ctx* ctx, int gid, const fsgc_matching_order* mos, int n, fsgc_result* results);
+
 /* Many (graph, pattern) tasks in one call; results in task order. */
 typedef struct fsgc_task {
   int32_t gid;
