@@ -726,6 +726,17 @@ int fsgc_graph_prepare(fsgc_ctx* c, int gid) {
   return FSGC_OK;
 }
 
+int fsgc_graph_prepare_all(fsgc_ctx* c, int gid) {
+  if (!c) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DevGraph* g = find_graph(c, gid);
+  if (!g) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", gid);
+  const int st = fsgc::prepare_all(*g, c->stream, &c->launches, c->work);
+  if (st != FSGC_OK) return fail(c, st, "graph preparation failed: %s", cudaGetErrorString(cudaGetLastError()));
+  return FSGC_OK;
+}
+
 int fsgc_graph_info_get(fsgc_ctx* c, int gid, fsgc_graph_info* out) {
   if (!c || !out) return FSGC_EINVAL;
   std::lock_guard<std::mutex> lk(c->mu);

@@ -1650,6 +1650,15 @@ int prepare_for_count(const fsgc_matching_order& mo, DevGraph& G, cudaStream_t s
   return cudaStreamSynchronize(s) == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
 }
 
+int prepare_all(DevGraph& G, cudaStream_t s, uint64_t* launches, DevWork& work) {
+  int st = prepare_graph(G, s, launches, work.small);
+  if (st == FSGC_OK && G.ngraphs == 0) st = ensure_chunk_table(G, s, launches, work.small + 9);
+  if (st == FSGC_OK) st = ensure_vertex_triangles(G, s, launches);
+  if (st == FSGC_OK && G.ngraphs == 0) st = ensure_entry_supports(G, s, launches);
+  if (st != FSGC_OK) return st;
+  return cudaStreamSynchronize(s) == cudaSuccess ? FSGC_OK : FSGC_ECUDA;
+}
+
 namespace {
 // Both pair kernels of the fringe-free-centre wedge core for a set of
 // patterns: endpoints of degree <= kWDvMax, then hub endpoints (cursors and

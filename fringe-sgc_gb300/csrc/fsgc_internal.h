@@ -145,6 +145,8 @@ int enqueue_count_set(std::vector<CountJob*>& jobs, cudaStream_t s, uint64_t* la
 // other streams only read the graph.
 int prepare_for_count(const fsgc_matching_order& mo, DevGraph& g, cudaStream_t s, uint64_t* launches,
                       DevWork& work);
+// Builds every per-graph structure any count could need, synchronously.
+int prepare_all(DevGraph& g, cudaStream_t s, uint64_t* launches, DevWork& work);
 // Scratch-arena bytes a count of `mo` on the prepared graph `g` grows to.
 size_t count_scratch_bytes(const fsgc_matching_order& mo, const DevGraph& g);
 

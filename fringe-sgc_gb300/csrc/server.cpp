@@ -12,7 +12,13 @@
 // Meanwhile the other workers admit and submit what arrives, so work from
 // different batches overlaps on the device and no query waits for a batch
 // that was already running when it arrived.  A batch the checks refuse is
-// re-run one query at a time, so that a bad query fails alone.  Latency is
+// re-run one query at a time, so that a bad query fails alone, and when a
+// count fails inside a batch the queries after it are re-run one at a time.
+// Registering a graph builds every derived structure any count could need
+// (orientation, supports, chunk table, per-vertex triangles, per-entry
+// supports), so no query builds one under the context lock while other lanes
+// wait, and the graph's device bytes count against the budget for as long as
+// it is registered, beside the lanes' work arenas.  Latency is
 // submission to completion.  Results are cached by (graph, matching-order
 // bytes): resident graphs never change and graph ids are never reused, so a
 // repeated query completes at submission without device work.
@@ -57,6 +63,7 @@ struct LaneSlot {
 struct fsgc_server {
   fsgc_ctx* ctx = nullptr;
   size_t budget = 0;
+  size_t resident = 0;    // device bytes of the registered graphs
   size_t held_total = 0;  // sum of LaneSlot::held
   int max_batch = 64;
   std::mutex mu;
@@ -92,7 +99,7 @@ bool admit(fsgc_server* s, LaneSlot& ls, std::vector<uint64_t>& batch) {
     const Query& q = s->queries[s->waiting.front()];
     const size_t nneed = std::max(need, q.footprint);
     const size_t mine = std::max(ls.held, nneed);
-    if (s->held_total - ls.held + mine > s->budget) break;
+    if (s->resident + s->held_total - ls.held + mine > s->budget) break;
     need = nneed;
     batch.push_back(q.ticket);
     s->waiting.pop_front();
@@ -169,9 +176,17 @@ void worker_loop(fsgc_server* s, int li) {
     };
     int st = fsgc_lane_submit(lane, tasks.data(), (int)tasks.size());
     if (st == FSGC_OK) {
-      for (size_t i = 0; i < batch.size(); i++) {
-        status[i] = (st == FSGC_OK) ? fsgc_lane_wait_task(lane, (int)i, &results[i]) : st;
-        st = status[i];
+      size_t i = 0;
+      for (; i < batch.size(); i++) {
+        status[i] = fsgc_lane_wait_task(lane, (int)i, &results[i]);
+        complete(i);
+        if (status[i] != FSGC_OK) break;
+      }
+      // a count failed inside the batch (its submission is abandoned): the
+      // queries after it run one at a time, so each gets its own outcome
+      for (i = i + 1; i < batch.size(); i++) {
+        status[i] = fsgc_lane_submit(lane, &tasks[i], 1);
+        if (status[i] == FSGC_OK) status[i] = fsgc_lane_wait(lane, &results[i]);
         complete(i);
       }
     } else if (batch.size() > 1) {
@@ -251,9 +266,16 @@ void fsgc_server_destroy(fsgc_server* s) {
 
 int fsgc_server_add_graph(fsgc_server* s, int gid) {
   if (!s) return FSGC_EINVAL;
-  const int st = fsgc_graph_prepare(s->ctx, gid);
+  int st = fsgc_graph_prepare_all(s->ctx, gid);
+  if (st != FSGC_OK) return st;
+  fsgc_graph_info info;
+  st = fsgc_graph_info_get(s->ctx, gid, &info);
   if (st != FSGC_OK) return st;
   std::lock_guard<std::mutex> lk(s->mu);
+  if (s->graphs.count(gid)) return FSGC_OK;
+  const size_t bytes = (size_t)std::max<int64_t>(0, info.device_bytes);
+  if (s->resident + s->held_total + bytes > s->budget) return FSGC_EBUSY;  // does not fit beside what is there
+  s->resident += bytes;
   s->graphs[gid] = 1;
   return FSGC_OK;
 }
@@ -352,7 +374,7 @@ int fsgc_server_stats_get(fsgc_server* s, fsgc_server_stats* out) {
   out->completed = s->completed;
   out->rounds = s->rounds;
   out->queued = s->waiting.size();
-  out->in_use_bytes = s->held_total;
+  out->in_use_bytes = s->held_total + s->resident;
   out->cache_hits = s->cache_hits;
   out->p50_ms = percentile(s->latencies, 0.50);
   out->p99_ms = percentile(s->latencies, 0.99);

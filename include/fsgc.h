@@ -149,6 +149,10 @@ int fsgc_graph_release(fsgc_ctx* ctx, int gid);
  * instead of on the first count that needs them (the reference's relabel and
  * worklist builders, src/fringeCount.cu:1221-1288, 617-663, 1167-1218). */
 int fsgc_graph_prepare(fsgc_ctx* ctx, int gid);
+/* Builds, now, every derived structure any count on this graph could need:
+ * the passes above plus the wedge core's chunk table, the per-vertex triangle
+ * counts and the per-entry supports (their bytes show in device_bytes). */
+int fsgc_graph_prepare_all(fsgc_ctx* ctx, int gid);
 
 typedef struct fsgc_graph_info {
   int32_t n;
@@ -250,10 +254,13 @@ int fsgc_task_footprint(fsgc_ctx* ctx, const fsgc_task* task, size_t* bytes);
  *      process per query: src/fringeCount.cu:2265-2331) ----
  * Continuous batching over `lanes` lanes of `ctx`, one worker thread each.
  * Graphs are uploaded to the context first and registered with
- * fsgc_server_add_graph (which prepares them).  Submitted queries wait in
- * arrival order.  Whenever a lane is free, its worker admits queries from the
- * head of the queue (at most `max_batch`) while the lanes' work arenas, with
- * this batch's need, fit `memory_budget`; it submits them to its lane and
+ * fsgc_server_add_graph, which builds every derived structure a count could
+ * need (fsgc_graph_prepare_all) and counts the graph's device bytes against
+ * `memory_budget` while it is registered (FSGC_EBUSY when it does not fit).
+ * Submitted queries wait in arrival order.  Whenever a lane is free, its
+ * worker admits queries from the head of the queue (at most `max_batch`)
+ * while the registered graphs and the lanes' work arenas, with this batch's
+ * need, fit `memory_budget`; it submits them to its lane and
  * completes them when they finish, while the other lanes keep admitting and
  * running queries that arrived in the meantime.  A query whose footprint alone
  * exceeds the budget is refused at submission (FSGC_EBUSY); a query that fails

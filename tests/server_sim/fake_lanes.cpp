@@ -4,8 +4,9 @@
 //
 // A task on graph `gid` needs a work arena of gid MiB and takes `mo.nodes`
 // milliseconds; its count is gid * 1000 + nodes.  A matching order with
-// nodes == 6 passes the submission checks and fails when counted; nodes == 0
-// or > 6 is malformed; graphs above 100 do not exist.  The fake records the
+// nodes == 6 fails the submission checks; startdeg == 99 passes them and
+// fails when its count is waited for; nodes == 0 or > 6 is malformed; graphs
+// above 100 do not exist.  The fake records the
 // peak sum of the lanes' arenas and the peak number of lanes counting at once.
 #include <algorithm>
 #include <atomic>
@@ -49,6 +50,15 @@ void sim_ctx_peaks(fsgc_ctx* c, size_t* peak_bytes, int* peak_busy) {
 }
 
 int fsgc_graph_prepare(fsgc_ctx*, int gid) { return (gid >= 1 && gid <= 100) ? FSGC_OK : FSGC_ENOTFOUND; }
+int fsgc_graph_prepare_all(fsgc_ctx* c, int gid) { return fsgc_graph_prepare(c, gid); }
+
+// Graphs hold no device memory except 90 and 91, which hold 40 MiB each.
+int fsgc_graph_info_get(fsgc_ctx*, int gid, fsgc_graph_info* out) {
+  if (gid < 1 || gid > 100) return FSGC_ENOTFOUND;
+  memset(out, 0, sizeof(*out));
+  out->device_bytes = (gid == 90 || gid == 91) ? (int64_t)40 << 20 : 0;
+  return FSGC_OK;
+}
 
 int fsgc_task_footprint(fsgc_ctx*, const fsgc_task* t, size_t* bytes) {
   if (malformed(t->mo)) return FSGC_EINVAL;
@@ -98,6 +108,13 @@ int fsgc_lane_submit(fsgc_lane* l, const fsgc_task* tasks, int n) {
 int fsgc_lane_wait_task(fsgc_lane* l, int i, fsgc_result* out) {
   if (!l || l->pending <= 0 || i < l->finished || i >= l->pending) return FSGC_ENOTFOUND;
   std::this_thread::sleep_until(l->done_at[(size_t)i]);
+  if (l->tasks[(size_t)i].mo.startdeg == 99) {
+    // a count that fails on the device: the submission is abandoned
+    l->pending = 0;
+    std::lock_guard<std::mutex> lk(l->ctx->mu);
+    l->ctx->busy--;
+    return FSGC_ECUDA;
+  }
   if (out) {
     memset(out, 0, sizeof(*out));
     out->count = out->raw_total = (uint64_t)l->tasks[(size_t)i].gid * 1000 + l->tasks[(size_t)i].mo.nodes;

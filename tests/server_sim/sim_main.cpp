@@ -150,6 +150,49 @@ int main() {
     }
     fsgc_server_destroy(srv);
   }
+  // 6. a count that fails inside a batch fails alone: the queries after it
+  //    run one at a time and keep their own results
+  {
+    fsgc_server* srv = nullptr;
+    CHECK(fsgc_server_create(ctx, 64 * MiB, 1, 8, &srv) == FSGC_OK, "create");
+    CHECK(fsgc_server_add_graph(srv, 4) == FSGC_OK, "add");
+    fsgc_matching_order slow = order(5, 80), a = order(2, 81), boom = order(3, 82), b = order(1, 83), c = order(4, 84);
+    boom.startdeg = 99;
+    uint64_t t0, t1, t2, t3, t4;
+    CHECK(fsgc_server_submit(srv, 4, &slow, &t0) == FSGC_OK, "submit");
+    CHECK(fsgc_server_submit(srv, 4, &a, &t1) == FSGC_OK, "submit");
+    CHECK(fsgc_server_submit(srv, 4, &boom, &t2) == FSGC_OK, "submit");
+    CHECK(fsgc_server_submit(srv, 4, &b, &t3) == FSGC_OK, "submit");
+    CHECK(fsgc_server_submit(srv, 4, &c, &t4) == FSGC_OK, "submit");
+    fsgc_result r;
+    CHECK(fsgc_server_wait(srv, t0, 10, &r, nullptr) == FSGC_OK && r.count == 4005, "slow");
+    CHECK(fsgc_server_wait(srv, t1, 10, &r, nullptr) == FSGC_OK && r.count == 4002, "before the failure");
+    CHECK(fsgc_server_wait(srv, t2, 10, &r, nullptr) == FSGC_ECUDA, "the failing count");
+    CHECK(fsgc_server_wait(srv, t3, 10, &r, nullptr) == FSGC_OK && r.count == 4001, "after the failure");
+    CHECK(fsgc_server_wait(srv, t4, 10, &r, nullptr) == FSGC_OK && r.count == 4004, "after the failure");
+    fsgc_server_destroy(srv);
+  }
+
+  // 7. registered graphs count against the budget: two 40 MiB graphs do not
+  //    fit a 64 MiB budget, and a query needing 30 MiB waits for room beside
+  //    the one that does
+  {
+    fsgc_server* srv = nullptr;
+    CHECK(fsgc_server_create(ctx, 64 * MiB, 2, 4, &srv) == FSGC_OK, "create");
+    CHECK(fsgc_server_add_graph(srv, 90) == FSGC_OK, "first 40 MiB graph");
+    CHECK(fsgc_server_add_graph(srv, 91) == FSGC_EBUSY, "second 40 MiB graph accepted");
+    CHECK(fsgc_server_add_graph(srv, 20) == FSGC_OK, "small graph");
+    fsgc_matching_order mo = order(2, 90);
+    uint64_t t;
+    CHECK(fsgc_server_submit(srv, 20, &mo, &t) == FSGC_OK, "submit");
+    fsgc_result r;
+    CHECK(fsgc_server_wait(srv, t, 10, &r, nullptr) == FSGC_OK && r.count == 20002, "count beside a resident graph");
+    fsgc_server_stats st;
+    fsgc_server_stats_get(srv, &st);
+    CHECK(st.in_use_bytes >= 40 * MiB, "resident bytes not reported");
+    fsgc_server_destroy(srv);
+  }
+
   size_t peak = 0;
   int peak_busy = 0;
   sim_ctx_peaks(ctx, &peak, &peak_busy);
