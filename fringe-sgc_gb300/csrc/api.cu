@@ -565,6 +565,63 @@ int fsgc_graph_from_device_csr(fsgc_ctx* c, int n, int64_t m, const int64_t* d_n
   return FSGC_OK;
 }
 
+int fsgc_graph_from_edges(fsgc_ctx* c, int n, int64_t nedges, const int32_t* pairs, int pairs_on_device, int* gid) {
+  if (!c || !gid || n < 1 || nedges < 0 || (nedges > 0 && !pairs)) return fail(c, FSGC_EINVAL, "bad edge-list arguments");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  const int* d_pairs = pairs;
+  int* owned = nullptr;
+  if (!pairs_on_device && nedges > 0) {
+    CK(cudaMallocAsync((void**)&owned, sizeof(int32_t) * 2 * (size_t)nedges, c->stream), "edge-list upload");
+    CK(cudaMemcpyAsync(owned, pairs, sizeof(int32_t) * 2 * (size_t)nedges, cudaMemcpyHostToDevice, c->stream),
+       "edge-list upload");
+    d_pairs = owned;
+  }
+  long long* off = nullptr;
+  int* adj = nullptr;
+  long long m = 0;
+  int st = fsgc::csr_from_device_edges(n, nedges, d_pairs, c->stream, &off, &adj, &m, c->work.small);
+  if (owned) cudaFreeAsync(owned, c->stream);
+  if (st != FSGC_OK) {
+    cudaStreamSynchronize(c->stream);
+    return fail(c, st, st == FSGC_EINVAL ? "edge list has a vertex id outside [0, n)" : "edge-list ingestion failed");
+  }
+  DevGraph* g = new DevGraph();
+  g->n = n;
+  g->m = m;
+  g->off = off;
+  g->adj = adj;
+  if (cudaMalloc((void**)&g->deg, sizeof(int) * (size_t)n) != cudaSuccess) {
+    free_graph(g);
+    cudaGetLastError();
+    return fail(c, FSGC_ENOMEM, "graph allocation");
+  }
+  g->bytes = sizeof(long long) * ((size_t)n + 1) + sizeof(int) * ((size_t)m + (size_t)n);
+  st = fsgc::graph_degrees(*g, c->stream, &c->launches, c->work.small);
+  if (st != FSGC_OK) {
+    free_graph(g);
+    return fail(c, st, "degree pass failed");
+  }
+  *gid = c->next_gid++;
+  c->graphs[*gid] = g;
+  return FSGC_OK;
+}
+
+int fsgc_graph_copy_csr(fsgc_ctx* c, int gid, int64_t* nindex, int32_t* nlist) {
+  if (!c || !nindex) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DevGraph* g = find_graph(c, gid);
+  if (!g) return fail(c, FSGC_ENOTFOUND, "unknown graph %d", gid);
+  if (g->m > 0 && !nlist) return fail(c, FSGC_EINVAL, "no list buffer");
+  CK(cudaMemcpyAsync(nindex, g->off, sizeof(long long) * ((size_t)g->n + 1), cudaMemcpyDeviceToHost, c->stream),
+     "graph read-back");
+  if (g->m > 0)
+    CK(cudaMemcpyAsync(nlist, g->adj, sizeof(int) * (size_t)g->m, cudaMemcpyDeviceToHost, c->stream), "graph read-back");
+  CK(cudaStreamSynchronize(c->stream), "graph read-back");
+  return FSGC_OK;
+}
+
 int fsgc_graph_load_egr(fsgc_ctx* c, const char* path, int* gid) {
   fsgc_host_csr h;
   const int st = fsgc_egr_read(path, &h);

@@ -145,6 +145,11 @@ int enqueue_count_set(std::vector<CountJob*>& jobs, cudaStream_t s, uint64_t* la
 // other streams only read the graph.
 int prepare_for_count(const fsgc_matching_order& mo, DevGraph& g, cudaStream_t s, uint64_t* launches,
                       DevWork& work);
+// Edge list (device pairs) -> cleaned CSR on the device (ingest.cu).  The
+// arrays are the caller's to keep (stream-ordered allocations); the list
+// array is padded by 16 bytes.  FSGC_EINVAL for an id outside [0, n).
+int csr_from_device_edges(int n, long long E, const int* d_pairs, cudaStream_t s, long long** off_out, int** adj_out,
+                          long long* m_out, u64* d_small);
 // Builds every per-graph structure any count could need, synchronously.
 int prepare_all(DevGraph& g, cudaStream_t s, uint64_t* launches, DevWork& work);
 // Scratch-arena bytes a count of `mo` on the prepared graph `g` grows to.

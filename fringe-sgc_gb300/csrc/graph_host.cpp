@@ -4,6 +4,10 @@
 // The ECLgraph layout follows the reference's reader (src/ECLgraph.h:58-85):
 // int32 node count, int32 edge count (directed entries), int32 nindex[n+1],
 // int32 nlist[m], optionally int32 eweight[m] (ignored, as fringeCount ignores it).
+// Graphs of 2^31 or more directed entries do not fit those int32 fields; they
+// are written in an extension of the layout: int32 n, int32 -1 (an edge count
+// the reference's reader refuses, so such a file is never misread as a
+// classic one), int64 m, int64 nindex[n+1], int32 nlist[m].
 //
 // Generators are counter-based (every random draw is a hash of seed and draw
 // index), so they produce identical graphs on any machine and thread count.
@@ -138,11 +142,36 @@ int fsgc_egr_read(const char* path, fsgc_host_csr* out) {
   memset(out, 0, sizeof(*out));
   FILE* f = fopen(path, "rb");
   if (!f) return FSGC_EIO;
-  int32_t n = 0, m = 0;
-  if (fread(&n, 4, 1, f) != 1 || fread(&m, 4, 1, f) != 1 || n < 1 || m < 0) {
+  int32_t n = 0, m32 = 0;
+  if (fread(&n, 4, 1, f) != 1 || fread(&m32, 4, 1, f) != 1 || n < 1 || m32 < -1) {
     fclose(f);
     return FSGC_EIO;
   }
+  if (m32 == -1) {  // the int64 extension
+    int64_t m = 0;
+    if (fread(&m, 8, 1, f) != 1 || m < 0) {
+      fclose(f);
+      return FSGC_EIO;
+    }
+    out->nindex = (int64_t*)malloc(sizeof(int64_t) * ((size_t)n + 1));
+    out->nlist = (int32_t*)malloc(sizeof(int32_t) * (m ? (size_t)m : 1));
+    if (!out->nlist || !out->nindex) {
+      fclose(f);
+      fsgc_host_csr_free(out);
+      return FSGC_ENOMEM;
+    }
+    if (fread(out->nindex, 8, (size_t)n + 1, f) != (size_t)n + 1 ||
+        (m > 0 && fread(out->nlist, 4, (size_t)m, f) != (size_t)m)) {
+      fclose(f);
+      fsgc_host_csr_free(out);
+      return FSGC_EIO;
+    }
+    fclose(f);
+    out->n = n;
+    out->m = m;
+    return FSGC_OK;
+  }
+  const int32_t m = m32;
   std::vector<int32_t> idx((size_t)n + 1);
   out->nlist = (int32_t*)malloc(sizeof(int32_t) * (m ? (size_t)m : 1));
   out->nindex = (int64_t*)malloc(sizeof(int64_t) * ((size_t)n + 1));
@@ -164,9 +193,22 @@ int fsgc_egr_read(const char* path, fsgc_host_csr* out) {
   return FSGC_OK;
 }
 
+int fsgc_egr_write64(const char* path, const fsgc_host_csr* g) {
+  if (!path || !g || !g->nindex || g->n < 1 || g->m < 0 || (g->m > 0 && !g->nlist)) return FSGC_EINVAL;
+  FILE* f = fopen(path, "wb");
+  if (!f) return FSGC_EIO;
+  const int32_t n = g->n, mark = -1;
+  const int64_t m = g->m;
+  bool ok = fwrite(&n, 4, 1, f) == 1 && fwrite(&mark, 4, 1, f) == 1 && fwrite(&m, 8, 1, f) == 1 &&
+            fwrite(g->nindex, 8, (size_t)n + 1, f) == (size_t)n + 1 &&
+            (m == 0 || fwrite(g->nlist, 4, (size_t)m, f) == (size_t)m);
+  ok = (fclose(f) == 0) && ok;
+  return ok ? FSGC_OK : FSGC_EIO;
+}
+
 int fsgc_egr_write(const char* path, const fsgc_host_csr* g) {
   if (!path || !g || !g->nindex || (g->m > 0 && !g->nlist)) return FSGC_EINVAL;
-  if (g->m > 2147483647LL) return FSGC_EUNSUPPORTED;
+  if (g->m > 2147483647LL) return fsgc_egr_write64(path, g);
   FILE* f = fopen(path, "wb");
   if (!f) return FSGC_EIO;
   const int32_t n = g->n, m = (int32_t)g->m;

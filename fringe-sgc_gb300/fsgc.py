@@ -99,6 +99,7 @@ def lib():
             "fsgc_predefined_name": (C.c_char_p, [I]),
             "fsgc_egr_read": (I, [C.c_char_p, C.POINTER(HostCSR)]),
             "fsgc_egr_write": (I, [C.c_char_p, C.POINTER(HostCSR)]),
+            "fsgc_egr_write64": (I, [C.c_char_p, C.POINTER(HostCSR)]),
             "fsgc_csr_validate": (I, [C.POINTER(HostCSR), C.c_char_p, I]),
             "fsgc_gen_rmat": (I, [I, I, C.c_double, C.c_double, C.c_double, U64, C.POINTER(HostCSR)]),
             "fsgc_gen_er": (I, [I, I64, U64, C.POINTER(HostCSR)]),
@@ -114,6 +115,9 @@ def lib():
             "fsgc_graph_from_csr": (I, [P, I, I64, P, P, C.POINTER(C.c_int)]),
             "fsgc_graph_from_csr32": (I, [P, I, I, P, P, C.POINTER(C.c_int)]),
             "fsgc_graph_from_device_csr": (I, [P, I, I64, P, P, C.POINTER(C.c_int)]),
+            "fsgc_graph_from_edges": (I, [P, I, I64, P, I, C.POINTER(C.c_int)]),
+            "fsgc_graph_copy_csr": (I, [P, I, P, P]),
+            "fsgc_graph_prepare_all": (I, [P, I]),
             "fsgc_graph_load_egr": (I, [P, C.c_char_p, C.POINTER(C.c_int)]),
             "fsgc_graph_release": (I, [P, I]),
             "fsgc_graph_prepare": (I, [P, I]),
@@ -258,9 +262,12 @@ def egr_read(path):
     return _take(h)
 
 
-def egr_write(path, g):
+def egr_write(path, g, int64=False):
+    """Writes the reference's .egr layout, or its int64 extension when the graph
+    needs it (m >= 2^31) or `int64` is set."""
     h = g.as_host_csr()
-    _check(lib().fsgc_egr_write(path.encode(), C.byref(h)), "egr_write")
+    fn = lib().fsgc_egr_write64 if int64 else lib().fsgc_egr_write
+    _check(fn(path.encode(), C.byref(h)), "egr_write")
 
 
 def validate(g):
@@ -336,6 +343,32 @@ class Context:
         _check(lib().fsgc_graph_from_device_csr(self.ptr, n, m, d_nindex, d_nlist, C.byref(gid)),
                "graph_from_device_csr", self.ptr)
         return gid.value
+
+    def upload_edges(self, n, pairs, on_device=False):
+        """Edge-list ingestion on the GPU (fsgc_graph_from_edges): `pairs` is
+        an (E, 2) int32 array, or a device pointer to 2E int32 when on_device
+        (then pass E as len via a tuple (ptr, E))."""
+        gid = C.c_int()
+        if on_device:
+            ptr, E = pairs
+        else:
+            arr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+            ptr, E = arr.ctypes.data, len(arr)
+        _check(lib().fsgc_graph_from_edges(self.ptr, n, E, ptr, 1 if on_device else 0, C.byref(gid)),
+               "graph_from_edges", self.ptr)
+        return gid.value
+
+    def download(self, gid):
+        """The resident graph's CSR, read back (a Graph)."""
+        info = self.info(gid)
+        idx = np.zeros(info.n + 1, np.int64)
+        adj = np.zeros(max(1, info.m), np.int32)
+        _check(lib().fsgc_graph_copy_csr(self.ptr, gid, idx.ctypes.data, adj.ctypes.data), "graph_copy_csr",
+               self.ptr)
+        return Graph(idx, adj[:info.m])
+
+    def prepare_all(self, gid):
+        _check(lib().fsgc_graph_prepare_all(self.ptr, gid), "graph_prepare_all", self.ptr)
 
     def load_egr(self, path):
         gid = C.c_int()

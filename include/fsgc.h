@@ -96,10 +96,15 @@ typedef struct fsgc_host_csr {
   int32_t* nlist;
 } fsgc_host_csr;
 
-/* readECLgraph (src/ECLgraph.h:58-85): int32 header and arrays; weights ignored. */
+/* readECLgraph (src/ECLgraph.h:58-85): int32 header and arrays; weights ignored.
+ * Also reads the int64 extension below. */
 int fsgc_egr_read(const char* path, fsgc_host_csr* out);
-/* Writes the same format (int32 offsets; fails with FSGC_EUNSUPPORTED if m >= 2^31). */
+/* Writes the same format; graphs of m >= 2^31 directed entries, which its int32
+ * fields cannot hold, in an extension: int32 n, int32 -1 (refused by the
+ * reference's reader), int64 m, int64 nindex[n+1], int32 nlist[m]. */
 int fsgc_egr_write(const char* path, const fsgc_host_csr* g);
+/* Writes the int64 extension whatever m is (for tests and tools). */
+int fsgc_egr_write64(const char* path, const fsgc_host_csr* g);
 /* Checks the reference's documented preconditions (src/fringeCount.cu:50-56):
  * sorted, duplicate-free, loop-free, symmetric lists. */
 int fsgc_csr_validate(const fsgc_host_csr* g, char* errbuf, int errlen);
@@ -144,6 +149,16 @@ int fsgc_graph_from_csr32(fsgc_ctx* ctx, int n, int m, const int32_t* nindex, co
 int fsgc_graph_from_device_csr(fsgc_ctx* ctx, int n, int64_t m, const int64_t* d_nindex, const int32_t* d_nlist,
                                int* gid);
 int fsgc_graph_load_egr(fsgc_ctx* ctx, const char* path, int* gid);
+/* Edge-list ingestion on the GPU (the reference has none: its loader reads a
+ * CSR that must already be clean, src/ECLgraph.h:58-85, src/fringeCount.cu:50-56):
+ * nedges undirected pairs (2 x int32 each, host memory, or device memory of
+ * the context's device when pairs_on_device) become the resident CSR with
+ * self loops dropped, duplicates merged, both directions and sorted lists --
+ * the same graph fsgc_csr_from_edges builds on the host.  FSGC_EINVAL for an
+ * id outside [0, n). */
+int fsgc_graph_from_edges(fsgc_ctx* ctx, int n, int64_t nedges, const int32_t* pairs, int pairs_on_device, int* gid);
+/* Copies a resident graph's CSR back to host buffers (nindex[n+1], nlist[m]). */
+int fsgc_graph_copy_csr(fsgc_ctx* ctx, int gid, int64_t* nindex, int32_t* nlist);
 int fsgc_graph_release(fsgc_ctx* ctx, int gid);
 /* Runs the loader's derived passes now (degree orientation, triangle supports)
  * instead of on the first count that needs them (the reference's relabel and

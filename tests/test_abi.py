@@ -150,3 +150,26 @@ def sys_path_bench():
     import sys
     if ROOT not in sys.path:
         sys.path.insert(0, ROOT)
+
+
+def test_egr_int64_extension_round_trip(tmp_path):
+    """Graphs of 2^31 or more directed entries are written in the int64
+    extension (int32 n, int32 -1, int64 m, int64 offsets, int32 lists); the
+    reader takes both layouts and the reference's own reader refuses the
+    extension's negative edge count (src/ECLgraph.h:64-66)."""
+    g = fsgc.gen_rmat(11, 8, seed=9)
+    p64, p32 = str(tmp_path / "g64.egr"), str(tmp_path / "g32.egr")
+    fsgc.egr_write(p64, g, int64=True)
+    fsgc.egr_write(p32, g)
+    raw = open(p64, "rb").read()
+    assert int.from_bytes(raw[0:4], "little") == g.n and int.from_bytes(raw[4:8], "little", signed=True) == -1
+    assert int.from_bytes(raw[8:16], "little") == g.m
+    assert len(raw) == 16 + 8 * (g.n + 1) + 4 * g.m
+    for p in (p64, p32):
+        h = fsgc.egr_read(p)
+        assert np.array_equal(h.nindex, g.nindex) and np.array_equal(h.nlist, g.nlist)
+    bad = str(tmp_path / "bad.egr")
+    with open(bad, "wb") as f:
+        f.write(raw[:40])  # truncated
+    with pytest.raises(fsgc.FsgcError):
+        fsgc.egr_read(bad)
