@@ -248,11 +248,25 @@ def job_value(patterns_per_rank, steps, world, seconds):
     return patterns_per_rank * world * steps / seconds
 
 
+def apply_tuning(ctx, g):
+    """The autotuner's values for this graph (fringe-sgc_gb300/tuning.json,
+    written by fringe-sgc_gb300/autotune.py on a GB300), else the defaults.
+    Returns what the line reports."""
+    import autotune
+    key = autotune.graph_key(g.n, g.m, int(g.degrees().max()))
+    values = autotune.load(os.path.join(ROOT, "fringe-sgc_gb300", "tuning.json"), key)
+    if values:
+        ctx.set_tuning(None, **values)
+        return {"source": "fringe-sgc_gb300/tuning.json (autotune.py)", "values": values}
+    return {"source": "defaults", "values": ctx.get_tuning().as_dict()}
+
+
 def run_gpu(args, rank, world):
     import fsgc
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = fsgc.Context(dev)
     g, gen_s = workload_graph(args.scale)
+    tuning = apply_tuning(ctx, g)
     mos = matching_orders(args.patterns)
     tasks_of = lambda gid: [(gid, mo) for _, mo in mos]  # noqa: E731
     # raw CSR resident in HBM for the device-resident measurement
@@ -342,6 +356,7 @@ def run_gpu(args, rank, world):
         "exact": exact,
         "cores": {name: int(r.core_type) for (name, _), r in zip(mos, ref_res)},
         "t_dev": t_dev, "t_e2e": t_e2e, "launches": launches, "clocks": clk.summary(), "gen_s": gen_s,
+        "tuning": tuning,
         "graph": {"n": g.n, "m": g.m, "max_degree": int(g.degrees().max())},
     }
     return out, g, mos, ctx
@@ -709,7 +724,8 @@ def main():
                    "per_pattern_ms": {k: round(v, 3) for k, v in out["per_task_ms"].items()},
                    "edges_per_s": {k: (round(v, 1) if v is not None else None)
                                    for k, v in edges_per_second(g.m, out["per_task_ms"]).items()},
-                   "counts": out["counts"], "exact_counts": out["exact"]},
+                   "counts": out["counts"], "exact_counts": out["exact"],
+                   "tuning": out.get("tuning")},
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * len(mos)},

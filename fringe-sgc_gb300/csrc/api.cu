@@ -515,6 +515,28 @@ int fsgc_ctx_flush_l2(fsgc_ctx* c, size_t bytes) {
   return FSGC_OK;
 }
 
+int fsgc_tuning_default(fsgc_tuning* out) {
+  if (!out) return FSGC_EINVAL;
+  *out = fsgc::DevWork().tune;
+  return FSGC_OK;
+}
+
+int fsgc_ctx_set_tuning(fsgc_ctx* c, const fsgc_tuning* t) {
+  if (!c || !t) return FSGC_EINVAL;
+  if (fsgc::check_tuning(*t) != FSGC_OK) return fail(c, FSGC_EINVAL, "tuning value out of range");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->work.tune = *t;
+  drop_set_graphs(c, -1);  // captured launches hold the old shapes
+  return FSGC_OK;
+}
+
+int fsgc_ctx_get_tuning(fsgc_ctx* c, fsgc_tuning* out) {
+  if (!c || !out) return FSGC_EINVAL;
+  std::lock_guard<std::mutex> lk(c->mu);
+  *out = c->work.tune;
+  return FSGC_OK;
+}
+
 int fsgc_ctx_set_exact_placements(fsgc_ctx* c, int on) {
   if (!c) return FSGC_EINVAL;
   std::lock_guard<std::mutex> lk(c->mu);
@@ -1042,6 +1064,7 @@ int fsgc_lane_submit(fsgc_lane* L, const fsgc_task* tasks, int ntasks) {
   std::lock_guard<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   if (L->pending > 0) return fail(c, FSGC_EBUSY, "lane has a submission in flight");
+  L->work.tune = c->work.tune;  // the context's method thresholds
   L->tasks.assign(tasks, tasks + ntasks);
   int st = plan_tasks(c, L->tasks.data(), ntasks, L->aut);
   if (st != FSGC_OK) return st;
@@ -1147,7 +1170,7 @@ int fsgc_task_footprint(fsgc_ctx* c, const fsgc_task* task, size_t* bytes) {
   if (pattern_too_large(task->mo, *g) || task->mo.nodes < 2) return FSGC_OK;
   const int st = fsgc::prepare_graph(*g, c->stream, &c->launches, c->work.small);
   if (st != FSGC_OK) return fail(c, st, "graph preparation failed: %s", cudaGetErrorString(cudaGetLastError()));
-  *bytes = fsgc::count_scratch_bytes(task->mo, *g);
+  *bytes = fsgc::count_scratch_bytes(task->mo, *g, c->work.tune);
   return FSGC_OK;
 }
 

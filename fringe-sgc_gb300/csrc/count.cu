@@ -281,6 +281,7 @@ struct TriParams {
   int relabel;  // roles by (deg, id) order (1) or by id (0)
   int kmax;     // largest out-degree (bitmap kernel)
   int stage;    // bitmap kernel: longest N(a) staged in shared memory (ints, multiple of 32)
+  int walk_ratio;  // bitmap kernel: walk N(b) when deg b <= walk_ratio * deg a
   Rot3 rot;
 };
 
@@ -444,9 +445,8 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
 // N(a) is staged in shared memory by a bulk copy when it fits p.stage ints.  A
 // row then takes the cheaper of two ways: walk N(b_i) from global memory
 // (coalesced) and look each entry up in the staged N(a), building the row in
-// a per-warp shared buffer, when deg b_i <= kTriWalkRatio * deg a; otherwise
+// a per-warp shared buffer, when deg b_i <= p.walk_ratio * deg a; otherwise
 // test each entry of N(a) by a binary search of N(b_i) (one ballot per 32).
-constexpr int kTriWalkRatio = 16;
 constexpr int kTriThreads = 256;
 constexpr int kBulkWaitPolls = 1 << 22;  // bounded wait for a bulk copy
 
@@ -532,7 +532,7 @@ __global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g
         const int* Nb = g.adj + g.off[b];
         const int db = g.deg[b];
         unsigned* row = bits + (size_t)i * W;
-        if (staged && db <= kTriWalkRatio * da) {
+        if (staged && (long long)db <= (long long)p.walk_ratio * da) {
           for (int w = lane; w < W; w += 32) wrow[w] = 0u;
           __syncwarp();
           // only N(b) entries inside [min N(a), max N(a)] can match
@@ -777,6 +777,7 @@ constexpr int kWedgeFuse = 4;
 struct WedgeSet {
   int np;
   int lim;
+  int small_max;  // endpoints up to this degree go to the SMALL kernel (<= kWDvMax)
   WedgeParams w[kWedgeFuse];
   u64* slot[kWedgeFuse];
 };
@@ -821,7 +822,7 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
     const int v = S.v;
     if (v >= g.n) break;
     const int dv = g.deg[v];
-    if (dv < ws.lim || (BIG ? dv <= kWDvMax : dv > kWDvMax)) {
+    if (dv < ws.lim || (BIG ? dv <= ws.small_max : dv > ws.small_max)) {
       __syncthreads();
       continue;
     }
@@ -1244,7 +1245,6 @@ __device__ u64 placement_sum_reference(const GenParams& p, int* venn) {
 }
 
 constexpr int kGenWarps = 4;  // warps per block in the general-core kernel
-constexpr int kGenLaneVennMax = 96;  // list entries up to which a lane builds its own Venn row
 
 struct GenWarp {
   int stack[6];
@@ -1564,11 +1564,11 @@ bool triangle_uses_bitmaps(const fsgc_matching_order&, const DevGraph& G, int mo
 // long an N(a) stage as fits a 72 KB block (three blocks per SM): 4 bytes per
 // staged entry plus one row bit per warp.  Returns the stage length (a multiple
 // of 32, or 0) and the block's dynamic shared memory.
-int triangle_stage(int kmax, size_t* smem) {
+int triangle_stage(int kmax, int stage_max, size_t* smem) {
   const long long fixed = 3LL * 4 * std::max(1, kmax);
   const long long budget = 72LL * 1024 - fixed - 16;
   long long stage = budget > 0 ? budget / (4 + (kTriThreads / 32) * 4 / 32) : 0;
-  stage = std::min<long long>(stage, 8192) & ~31LL;
+  stage = std::min<long long>(stage, std::min(8192, std::max(0, stage_max))) & ~31LL;
   if (stage < 64) stage = 0;
   *smem = (size_t)(4 * (stage + 4) + 4 * (stage / 32) * (kTriThreads / 32) + fixed);
   return (int)stage;
@@ -1586,7 +1586,7 @@ struct Needs {
   size_t scratch = 0;        // arena bytes (hub cursors, triangle bitmaps)
 };
 
-Needs needs_of(const fsgc_matching_order& mo, const DevGraph& G) {
+Needs needs_of(const fsgc_matching_order& mo, const DevGraph& G, const fsgc_tuning& t) {
   Needs nd;
   if (mo.nodes < 2 || mo.nodes > FSGC_MAX_CORE) return nd;
   if (mo.nodes == 2) {
@@ -1606,7 +1606,7 @@ Needs needs_of(const fsgc_matching_order& mo, const DevGraph& G) {
     }
     if (f[IUVW] == 0 && f[IUV] == 0 && f[IUW] == 0 && f[IU] == 0) {
       nd.chunk_table = true;
-      if (G.maxdeg > kWDvMax) {
+      if (G.maxdeg > std::min(kWDvMax, std::max(16, t.wedge_small_max_degree))) {
         const long long gs = G.maxdeg;
         nd.scratch = (size_t)sm_count() * ((size_t)2 * gs * sizeof(long long) + (size_t)(gs + 1) * sizeof(int));
       }
@@ -1627,14 +1627,24 @@ Needs needs_of(const fsgc_matching_order& mo, const DevGraph& G) {
 }
 }  // namespace
 
-size_t count_scratch_bytes(const fsgc_matching_order& mo, const DevGraph& G) { return needs_of(mo, G).scratch; }
+size_t count_scratch_bytes(const fsgc_matching_order& mo, const DevGraph& G, const fsgc_tuning& t) {
+  return needs_of(mo, G, t).scratch;
+}
+
+int check_tuning(const fsgc_tuning& t) {
+  const bool ok = t.wedge_small_max_degree >= 16 && t.wedge_small_max_degree <= kWDvMax && t.triangle_walk_ratio >= 0 &&
+                  t.triangle_walk_ratio <= (1 << 20) && t.triangle_stage_max >= 0 && t.triangle_stage_max <= 8192 &&
+                  t.triangle_stage_max % 32 == 0 && t.general_lane_venn_max >= 0 &&
+                  t.general_lane_venn_max <= (1 << 20) && t.general_blocks_per_sm >= 1 && t.general_blocks_per_sm <= 16;
+  return ok ? FSGC_OK : FSGC_EINVAL;
+}
 
 int prepare_for_count(const fsgc_matching_order& mo, DevGraph& G, cudaStream_t s, uint64_t* launches,
                       DevWork& work) {
   if (mo.nodes < 2) return FSGC_OK;
   int st = prepare_graph(G, s, launches, work.small);
   if (st != FSGC_OK) return st;
-  const Needs nd = needs_of(mo, G);
+  const Needs nd = needs_of(mo, G, work.tune);
   if (nd.chunk_table) {
     st = ensure_chunk_table(G, s, launches, work.small + 9);
     if (st != FSGC_OK) return st;
@@ -1664,7 +1674,7 @@ namespace {
 // patterns: endpoints of degree <= kWDvMax, then hub endpoints (cursors and
 // segment offsets in the work arena).
 template <int NP, class A>
-int launch_wedge_set(DevGraph& G, const GView& gv, const WedgeSet& ws, cudaStream_t s, uint64_t* launches,
+int launch_wedge_set(DevGraph& G, const GView& gv, const WedgeSet& ws0, cudaStream_t s, uint64_t* launches,
                      DevWork& work) {
   int* q1 = reinterpret_cast<int*>(work.small + 7);
   int* q2 = reinterpret_cast<int*>(work.small + 8);
@@ -1673,13 +1683,15 @@ int launch_wedge_set(DevGraph& G, const GView& gv, const WedgeSet& ws, cudaStrea
   const ChunkTable tab{G.ctab_id, G.ctab_pos, G.ctab_K};
   cudaMemsetAsync(q1, 0, 2 * sizeof(u64), s);
   const int blocks = sm_count();
+  WedgeSet ws = ws0;
+  ws.small_max = std::min(kWDvMax, std::max(16, work.tune.wedge_small_max_degree));
   {
     const size_t smem = sizeof(WedgeSmem<false>);
     cudaFuncSetAttribute(wedge_chunk_kernel<false, NP, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     wedge_chunk_kernel<false, NP, A><<<blocks, kWThreads, smem, s>>>(gv, ws, q1, nullptr, nullptr, 0, tab);
     *launches += 1;
   }
-  if (G.maxdeg > kWDvMax) {
+  if (G.maxdeg > ws.small_max) {
     // hub endpoints: cursors (2 x int64) and segment offsets (int32) per block
     const long long gs = G.maxdeg;
     const size_t need = (size_t)blocks * ((size_t)2 * gs * sizeof(long long) + (size_t)(gs + 1) * sizeof(int));
@@ -1702,7 +1714,8 @@ int launch_triangle_set(DevGraph& G, const GView& gv, TriParams tp, const TriSet
                         uint64_t* launches, DevWork& work) {
   size_t smem = 0;
   tp.kmax = (int)G.max_outdeg;
-  tp.stage = triangle_stage(tp.kmax, &smem);
+  tp.stage = triangle_stage(tp.kmax, work.tune.triangle_stage_max, &smem);
+  tp.walk_ratio = std::max(0, work.tune.triangle_walk_ratio);
   long long per_block;
   int blocks;
   triangle_bitmap_geometry(G, &per_block, &blocks);
@@ -1888,10 +1901,10 @@ int enqueue_count_a(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& 
     }
   }
   gp->nslots = ns;
-  gp->lane_venn_max = kGenLaneVennMax;
+  gp->lane_venn_max = std::max(0, work.tune.general_lane_venn_max);
   auto* queue = reinterpret_cast<unsigned long long*>(work.small + 5);
   cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
-  const int blocks = sm_count() * 8;
+  const int blocks = sm_count() * std::min(16, std::max(1, work.tune.general_blocks_per_sm));
   // the placement walk's state is sized by the step count
   if (ns <= 32) general_core_kernel<32, A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
   else if (ns <= 64) general_core_kernel<64, A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
@@ -2064,6 +2077,7 @@ WedgeSet single_wedge(int f_v, int f_vw, int f_w, int lim, int minsum, u64* slot
   memset(&ws, 0, sizeof(ws));
   ws.np = 1;
   ws.lim = lim;
+  ws.small_max = kWDvMax;
   ws.w[0] = WedgeParams{f_v, f_vw, f_w, lim, minsum};
   ws.slot[0] = slot;
   return ws;

@@ -93,6 +93,7 @@ struct DevWork {
   u64* small = nullptr;  // 32 u64; small[kErrWord] collects kernel error bits
   Scratch tri;
   u64* h_err = nullptr;  // pinned host copy of small[kErrWord], refreshed after kernels that can set it
+  fsgc_tuning tune = {2048, 16, 8192, 96, 8};
 };
 constexpr int kErrWord = 10;
 
@@ -153,6 +154,8 @@ int csr_from_device_edges(int n, long long E, const int* d_pairs, cudaStream_t s
 // Builds every per-graph structure any count could need, synchronously.
 int prepare_all(DevGraph& g, cudaStream_t s, uint64_t* launches, DevWork& work);
 // Scratch-arena bytes a count of `mo` on the prepared graph `g` grows to.
-size_t count_scratch_bytes(const fsgc_matching_order& mo, const DevGraph& g);
+size_t count_scratch_bytes(const fsgc_matching_order& mo, const DevGraph& g, const fsgc_tuning& t);
+// FSGC_EINVAL unless every field of `t` is in its documented range.
+int check_tuning(const fsgc_tuning& t);
 
 }  // namespace fsgc

@@ -118,6 +118,9 @@ def lib():
             "fsgc_graph_from_edges": (I, [P, I, I64, P, I, C.POINTER(C.c_int)]),
             "fsgc_graph_copy_csr": (I, [P, I, P, P]),
             "fsgc_graph_prepare_all": (I, [P, I]),
+            "fsgc_tuning_default": (I, [C.POINTER(Tuning)]),
+            "fsgc_ctx_set_tuning": (I, [P, C.POINTER(Tuning)]),
+            "fsgc_ctx_get_tuning": (I, [P, C.POINTER(Tuning)]),
             "fsgc_graph_load_egr": (I, [P, C.c_char_p, C.POINTER(C.c_int)]),
             "fsgc_graph_release": (I, [P, I]),
             "fsgc_graph_prepare": (I, [P, I]),
@@ -201,6 +204,22 @@ def predefined_pattern(number):
 
 
 # ----------------------------------------------------------------- host graphs
+class Tuning(C.Structure):
+    """fsgc_tuning: method thresholds and launch shapes (speed only, never results)."""
+    _fields_ = [("wedge_small_max_degree", C.c_int32), ("triangle_walk_ratio", C.c_int32),
+                ("triangle_stage_max", C.c_int32), ("general_lane_venn_max", C.c_int32),
+                ("general_blocks_per_sm", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+    @classmethod
+    def default(cls):
+        t = cls()
+        _check(lib().fsgc_tuning_default(C.byref(t)), "tuning_default")
+        return t
+
+
 class Graph:
     """Host CSR as numpy arrays: nindex int64[n+1], nlist int32[m]."""
 
@@ -366,6 +385,18 @@ class Context:
         _check(lib().fsgc_graph_copy_csr(self.ptr, gid, idx.ctypes.data, adj.ctypes.data), "graph_copy_csr",
                self.ptr)
         return Graph(idx, adj[:info.m])
+
+    def get_tuning(self):
+        t = Tuning()
+        _check(lib().fsgc_ctx_get_tuning(self.ptr, C.byref(t)), "get_tuning", self.ptr)
+        return t
+
+    def set_tuning(self, t=None, **fields):
+        """Sets the context's method thresholds: a Tuning, or fields over the current ones."""
+        cur = t if t is not None else self.get_tuning()
+        for k, v in fields.items():
+            setattr(cur, k, int(v))
+        _check(lib().fsgc_ctx_set_tuning(self.ptr, C.byref(cur)), "set_tuning", self.ptr)
 
     def prepare_all(self, gid):
         _check(lib().fsgc_graph_prepare_all(self.ptr, gid), "graph_prepare_all", self.ptr)

@@ -139,6 +139,25 @@ int fsgc_ctx_synchronize(fsgc_ctx* ctx);
  * placements; 1 sums the exact number.  Other core types are unaffected. */
 int fsgc_ctx_set_exact_placements(fsgc_ctx* ctx, int on);
 
+/* Method thresholds and launch shapes of the counting kernels (no counterpart
+ * in the reference, whose thresholds are compile-time constants,
+ * src/fringeCount.cu:70, 80-84, 1237, 1328-1334, 1797-1804).  They change speed,
+ * never results.  fringe-sgc_gb300/autotune.py picks them per graph by timing. */
+typedef struct fsgc_tuning {
+  int32_t wedge_small_max_degree; /* wedge pairs: endpoints up to this degree (16..2048) count in the
+                                     shared-memory kernel, higher ones in the hub kernel */
+  int32_t triangle_walk_ratio;    /* triangle bitmaps: a row walks N(b) against the staged N(a) when
+                                     deg b <= ratio * deg a, else searches N(b) (0: always search) */
+  int32_t triangle_stage_max;     /* longest N(a) staged in shared memory by bulk copy (0..8192, x32) */
+  int32_t general_lane_venn_max;  /* general core: a lane builds its own Venn row up to this many
+                                     list entries, longer rows are built by the whole warp */
+  int32_t general_blocks_per_sm;  /* general core: resident blocks of 4 warps per SM (1..16) */
+} fsgc_tuning;
+/* Defaults: 2048, 16, 8192, 96, 8. */
+int fsgc_tuning_default(fsgc_tuning* out);
+int fsgc_ctx_set_tuning(fsgc_ctx* ctx, const fsgc_tuning* t);
+int fsgc_ctx_get_tuning(fsgc_ctx* ctx, fsgc_tuning* out);
+
 /* ---- resident graphs (CSR upload + loader: src/fringeCount.cu:2286-2297) ---- */
 
 /* Uploads a host CSR (offsets 64-bit) and prepares it for counting. */
