@@ -173,3 +173,25 @@ def test_egr_int64_extension_round_trip(tmp_path):
         f.write(raw[:40])  # truncated
     with pytest.raises(fsgc.FsgcError):
         fsgc.egr_read(bad)
+
+
+def test_recorded_reference_counts_are_for_the_bench_graph_and_patterns():
+    """tests/golden/reference_rmat<scale>.json: the reference's own kernels'
+    counts on the benchmark graph; their graph sizes equal the generator's and
+    their matching orders the reference CLI's."""
+    import glob
+    import json
+    import refrun
+    files = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "reference_rmat*.json")))
+    assert len(files) >= 4
+    mos = refrun.workload_matching_orders()
+    for p in files:
+        rec = json.load(open(p))
+        gr = rec["graph"]
+        assert len(rec["patterns"]) == 8 and rec["gpu"] and "GB300" in rec["gpu"]
+        for name, r in rec["patterns"].items():
+            assert bytes.fromhex(r["mo"]) == mos[name], (p, name)
+            assert int(r["count"]) == int(r["raw"]) // r["aut"]
+        if gr["scale"] <= 18:
+            g = fsgc.gen_rmat(gr["scale"], gr["edge_factor"], gr["a"], gr["b"], gr["c"], gr["seed"])
+            assert (g.n, g.m) == (gr["n"], gr["m_directed"])

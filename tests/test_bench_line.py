@@ -73,7 +73,8 @@ def test_reference_arm_line(monkeypatch, capsys):
     """The reference arm's line: the reference's kernels' times (faked here),
     full passes repeated within the budget, the first ones untimed."""
     calls = _fake_refrun(monkeypatch, 250.0)
-    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "2", "--warmup", "3"])
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "2", "--warmup", "3",
+                                      "--ref-budget", "100000"])
     bench.main()
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unit"] == "patterns/s"
@@ -83,6 +84,30 @@ def test_reference_arm_line(monkeypatch, capsys):
                            "d2h_bytes_per_step": 0}
     assert line["cpu_baseline"]["kind"] == "reference" and line["config"]["value_bound"] is None
     assert line["config"]["counts"]["edge_5_5"]["count"] == "5"
+
+
+def test_reference_arm_takes_recorded_times_for_patterns_beyond_its_budget(monkeypatch, capsys):
+    """With the recorded RMAT-22 run, the shortest patterns run first and the
+    ones whose recorded time does not fit the budget are counted at that time."""
+    rec = bench.reference_golden(22)
+    assert rec is not None
+    ran = []
+    import refrun
+    _fake_refrun(monkeypatch, 0.0)
+
+    def run(egr, paths, timeout=None):
+        ran.append(paths[0])
+        return [{"core": 1, "aut": 1, "raw": 1, "count": 1, "ms": 100.0}]
+    monkeypatch.setattr(refrun, "run", run)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0",
+                                      "--ref-budget", "300"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["steps"] == 0 and line["config"]["value_bound"].startswith("upper")
+    skipped = [k for k, v in rec["patterns"].items() if v["ms"] > 200000]
+    assert len(ran) == 8 - len(skipped) and all(k in line["config"]["value_bound"] for k in skipped)
+    want = 8 / ((8 - len(skipped)) * 0.1 + sum(rec["patterns"][k]["ms"] / 1000.0 for k in skipped))
+    assert line["value"] == pytest.approx(want)
 
 
 def test_reference_arm_stops_within_its_budget(monkeypatch, capsys):
@@ -98,6 +123,7 @@ def test_reference_arm_stops_within_its_budget(monkeypatch, capsys):
         return [{"core": 3, "aut": 1, "raw": 1, "count": 1, "ms": 60000.0}]
     _fake_refrun(monkeypatch, 0.0)
     monkeypatch.setattr(refrun, "run", run)
+    monkeypatch.setattr(bench, "reference_golden", lambda scale: None)  # no recorded run to predict from
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "20", "--warmup", "5",
                                       "--ref-budget", "700"])
     bench.main()
