@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g
       for (int i = threadIdx.x; i < k; i += blockDim.x) {
         const int b = g.oadj[ob + i];
         outl[i] = b;
-        pos[i] = lower_bound_dev(Na, da, b);
+        pos[i] = lower_bound_any(Na, da, b);  // Na may be the shared-memory stage
         rowpop[i] = (int)g.osup[ob + i];  // |N(a) & N(b_i)| is the edge's support
       }
       // bitmaps: row i = N(a) & N(b_i), skipped when the edge closes no triangle

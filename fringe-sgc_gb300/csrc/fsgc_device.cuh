@@ -65,7 +65,8 @@ __host__ __device__ inline u64 nck_ref(int n, int k, const DivMagic* tab) {
 }
 
 // ----------------------------------------------------------------------------
-// Sorted-list helpers.  Lists are ascending int32 runs in global memory.
+// Sorted-list helpers.  Lists are ascending int32 runs in global memory (the
+// read-only loads below take global addresses only).
 
 // true if x occurs in a[0..len)
 __device__ __forceinline__ bool bsearch_has(const int* __restrict__ a, int len, int x) {
@@ -97,6 +98,18 @@ __device__ __forceinline__ int lower_bound_dev(const int* __restrict__ a, int le
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
     if (__ldg(a + mid) < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// number of elements < x in a[0..len) with plain loads: for lists that may sit
+// in shared memory (the __ldg searches above take global addresses only)
+__device__ __forceinline__ int lower_bound_any(const int* a, int len, int x) {
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1;
     else hi = mid;
   }
   return lo;
