@@ -317,8 +317,9 @@ int fsgc_server_submit(fsgc_server* s, int gid, const fsgc_matching_order* mo, u
   size_t fp = 0;
   const int st = fsgc_task_footprint(s->ctx, &task, &fp);
   if (st != FSGC_OK) return st;
-  if (fp > s->budget) return FSGC_EBUSY;  // can never be admitted
   std::lock_guard<std::mutex> lk(s->mu);
+  // can never be admitted beside the registered graphs
+  if (s->resident + fp > s->budget) return FSGC_EBUSY;
   Query q;
   q.ticket = s->next_ticket++;
   q.gid = gid;

@@ -98,18 +98,25 @@ def test_bad_query_fails_alone_and_admission_refuses(ctx):
         assert ctx.count(hid, wedge).core_type == 3
         need = fsgc.task_footprint(ctx, hid, wedge)
         assert need > 0
-        with fsgc.Server(ctx, memory_budget=need - 1, lanes=2, max_batch=8) as tiny:
+        # the registered graph's device bytes count against the budget too
+        ctx.prepare_all(hid)
+        resident = ctx.info(hid).device_bytes
+        with fsgc.Server(ctx, memory_budget=resident + need - 1, lanes=2, max_batch=8) as tiny:
             tiny.add_graph(hid)
             t = C.c_uint64()
             st = fsgc.lib().fsgc_server_submit(tiny.ptr, hid, C.byref(wedge), C.byref(t))
             assert st == 8  # FSGC_EBUSY: footprint above the whole budget
         # a budget for one such query at a time: they queue and all complete
-        with fsgc.Server(ctx, memory_budget=need, lanes=3, max_batch=1) as one:
+        with fsgc.Server(ctx, memory_budget=resident + need, lanes=3, max_batch=1) as one:
             one.add_graph(hid)
             ts = [one.submit(hid, wedge) for _ in range(6)]
-            outs = [one.wait(t)[0].count for t in ts]
+            outs = [one.wait(t, timeout_s=120)[0].count for t in ts]
             assert outs == [ctx.count(hid, wedge).count] * 6
-            assert one.stats().in_use_bytes <= need
+            assert one.stats().in_use_bytes <= resident + need
+        # a graph that does not fit beside the registered ones is refused
+        with fsgc.Server(ctx, memory_budget=resident - 1, lanes=1, max_batch=1) as small:
+            with pytest.raises(fsgc.FsgcError):
+                small.add_graph(hid)
         ctx.release(hid)
     finally:
         ctx.release(gid)
