@@ -457,6 +457,26 @@ def run_packed(args):
     ctx.close()
 
 
+def per_match_family(mo):
+    """True for the patterns whose kernels evaluate a formula per core match
+    with a per-match intersection: general cores (4-6 core vertices) and wedge
+    cores whose centre carries fringes (the reference's general_wedge_core,
+    src/fringeCount.cu:1513-1650).  Their work grows with the number of
+    wedges or core paths, one to two orders of magnitude per two RMAT scales."""
+    b = mo.to_bytes()
+    nodes = b[0]
+    if nodes >= 4:
+        return True
+    if nodes != 3 or bin(b[9]).count("1") != 1:
+        return False
+    f = [0] * 8
+    for i in range(b[1]):
+        f[b[13 + i] & 7] = b[76 + i]
+    if b[9] == 2:  # centre is B
+        f[1], f[2], f[5], f[6] = f[2], f[1], f[6], f[5]
+    return bool(f[7] or f[3] or f[5] or f[1])
+
+
 def run_mixed(args):
     """Batching on one graph: `--mixed-patterns` seeded patterns drawn as the
     batching configuration describes (core from edge, wedge, triangle,
@@ -468,16 +488,17 @@ def run_mixed(args):
                them into a CUDA graph, the timed calls replay it
       single   one fsgc_count per pattern (one query per launch)
 
-    Patterns whose decomposed core has four or more vertices (general cores)
-    enumerate every ordered core match and every fringe placement; their
-    work grows by one to two orders of magnitude per two RMAT scales, so they
-    run on the RMAT graph of scale --general-scale, with the same two modes.
-    Every batched count equals its single count."""
+    Patterns whose kernels evaluate a formula per core match with a
+    per-match intersection (general cores, and wedge cores whose centre
+    carries fringes: per_match_family) have work that grows by one to two
+    orders of magnitude per two RMAT scales, so they run on the RMAT graph of
+    scale --general-scale, with the same two modes.  Every batched count equals
+    its single count."""
     import fsgc
     ctx = fsgc.Context(0)
     pats = draw_patterns(args.mixed_patterns, 20251208, max_core=6)
-    small = [(n, mo) for n, mo in pats if mo.nodes <= 3]
-    general = [(n, mo) for n, mo in pats if mo.nodes >= 4]
+    small = [(n, mo) for n, mo in pats if not per_match_family(mo)]
+    general = [(n, mo) for n, mo in pats if per_match_family(mo)]
 
     def measure(scale, group):
         t = time.time()
@@ -518,9 +539,9 @@ def run_mixed(args):
             "value": main_part["batched_queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
             "warmup": max(2, args.warmup), "ms_per_step": main_part["batched_ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": f"{args.mixed_patterns} seeded mixed patterns (seed 20251208); the "
-                                   f"{len(small)} with cores of at most 3 vertices on RMAT scale {args.mixed_scale}, "
-                                   f"the {len(general)} general cores on RMAT scale {args.general_scale}",
+            "config": {"workload": f"{args.mixed_patterns} seeded mixed patterns (seed 20251208); "
+                                   f"{len(small)} on RMAT scale {args.mixed_scale}; the {len(general)} general "
+                                   f"cores and fringed-centre wedges on RMAT scale {args.general_scale}",
                        "main": main_part, "general": gen_part},
             "one_query_per_launch": {"value": main_part["single_queries_per_s"], "unit": "queries/s",
                                      "ms_per_step": main_part["single_ms"]},
@@ -730,7 +751,8 @@ def main():
                          "one graph; packed: batching across graphs; serve: the serving loop")
     ap.add_argument("--mixed-patterns", type=int, default=64, help="mixed: patterns drawn")
     ap.add_argument("--mixed-scale", type=int, default=24, help="mixed: RMAT scale for cores of <= 3 vertices")
-    ap.add_argument("--general-scale", type=int, default=12, help="mixed: RMAT scale for general cores")
+    ap.add_argument("--general-scale", type=int, default=12,
+                    help="mixed: RMAT scale for general cores and fringed-centre wedges")
     ap.add_argument("--graphs", type=int, default=256, help="packed: member graphs")
     ap.add_argument("--nmax", type=int, default=50000, help="packed: largest member size")
     ap.add_argument("--serve-scales", default="6,7,8,9,10,11,12,13", help="serve: RMAT scales")

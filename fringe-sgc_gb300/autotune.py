@@ -33,7 +33,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 CANDIDATES = {
     "wedge_small_max_degree": [256, 512, 1024, 2048],
-    "triangle_walk_ratio": [0, 4, 16, 64],
+    "triangle_walk_ratio": [0, 1, 2, 4, 16],
     "triangle_stage_max": [0, 2048, 8192],
     "general_lane_venn_max": [0, 32, 96, 256, 1 << 20],
     "general_blocks_per_sm": [2, 4, 8, 12],
