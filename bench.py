@@ -477,6 +477,24 @@ def per_match_family(mo):
     return bool(f[7] or f[3] or f[5] or f[1])
 
 
+def placement_bound(mo):
+    """Upper bound on the fringe placements a general core enumerates per core
+    match: per anchor set, multisets of its fringes over the regions that
+    contain it."""
+    from math import comb
+    b = mo.to_bytes()
+    sets = b[1]
+    anch, fcnt = b[13:13 + sets], b[76:76 + sets]
+    top = 0
+    for a in anch:
+        top |= a
+    bound = 1
+    for a, f in zip(anch, fcnt):
+        regions = 1 << (bin(top).count("1") - bin(a).count("1"))
+        bound *= comb(regions + f - 1, f)
+    return bound
+
+
 def run_mixed(args):
     """Batching on one graph: `--mixed-patterns` seeded patterns drawn as the
     batching configuration describes (core from edge, wedge, triangle,
@@ -492,21 +510,38 @@ def run_mixed(args):
     per-match intersection (general cores, and wedge cores whose centre
     carries fringes: per_match_family) have work that grows by one to two
     orders of magnitude per two RMAT scales, so they run on the RMAT graph of
-    scale --general-scale, with the same two modes.  Every batched count equals
-    its single count."""
+    scale --general-scale, with the same two modes, cheapest first by their
+    fringe-placement bound, within --general-budget seconds of single counts;
+    the rest are listed, not timed (a general core enumerates every fringe
+    placement of every core match, and for drawn patterns with many anchor
+    sets that is billions of steps even on a 64-vertex graph).  Every batched
+    count equals its single count."""
     import fsgc
     ctx = fsgc.Context(0)
     pats = draw_patterns(args.mixed_patterns, 20251208, max_core=6)
     small = [(n, mo) for n, mo in pats if not per_match_family(mo)]
     general = [(n, mo) for n, mo in pats if per_match_family(mo)]
 
-    def measure(scale, group):
+    def measure(scale, group, budget_s=None):
         t = time.time()
         g = fsgc.gen_rmat(scale, RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], RMAT["seed"])
         gen_s = time.time() - t
         gid = ctx.upload(g)
         ctx.prepare(gid)
         tuning = apply_tuning(ctx, g)
+        not_timed = []
+        if budget_s is not None:
+            # cheapest first by the fringe-placement enumeration bound; what
+            # does not fit the budget is listed, not timed
+            group = sorted(group, key=lambda p: (p[1].nodes, placement_bound(p[1])))
+            kept, t0 = [], time.time()
+            for name, mo in group:
+                if time.time() - t0 > budget_s:
+                    not_timed.append(name)
+                    continue
+                ctx.count(gid, mo)
+                kept.append((name, mo))
+            group = kept
         mos = [mo for _, mo in group]
         single = [ctx.count(gid, mo) for mo in mos]  # also builds every per-graph structure
         ctx.synchronize()
@@ -530,11 +565,12 @@ def run_mixed(args):
                 "batched_queries_per_s": len(mos) / t_batched, "batched_ms": t_batched * 1000,
                 "single_queries_per_s": len(mos) / t_single, "single_ms": t_single * 1000,
                 "batched_over_single": t_single / t_batched, "single_per_pattern_ms": per, "tuning": tuning,
-                "counts": {name: str(r.count) for (name, _), r in zip(group, single)}}
+                "counts": {name: str(r.count) for (name, _), r in zip(group, single)},
+                "not_timed": not_timed}
 
     launches0 = ctx.launches
     main_part = measure(args.mixed_scale, small)
-    gen_part = measure(args.general_scale, general) if general else None
+    gen_part = measure(args.general_scale, general, args.general_budget) if general else None
     line = {"metric": "queries/s, mixed patterns on one graph (batched in shared passes from a captured CUDA graph)",
             "value": main_part["batched_queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
             "warmup": max(2, args.warmup), "ms_per_step": main_part["batched_ms"], "higher_is_better": True,
@@ -566,7 +602,11 @@ def run_serve(args):
               for sc in scales]
     gen_s = time.time() - t
     gids = [ctx.upload(g) for g in graphs]
-    pats = draw_patterns(64, 20251206, max_core=3)
+    graph_sizes = [(g.n, g.m) for g in graphs]
+    del graphs  # the host copies (tens of GB at the larger scales)
+    # per-match families (general cores, fringed-centre wedges) are left out:
+    # at these scales one such query enumerates 10^12 and more core matches
+    pats = [(n, mo) for n, mo in draw_patterns(64, 20251206, max_core=3) if not per_match_family(mo)]
     rng = np.random.default_rng(20251207)
     nq = args.queries
     qs = [(int(rng.integers(len(gids))), int(rng.integers(len(pats)))) for _ in range(nq)]
@@ -606,19 +646,24 @@ def run_serve(args):
     poisson = serve(args.lanes, 64, True)
     launches = ctx.launches - launches0
     print(f"serve: poisson {poisson}", file=sys.stderr, flush=True)
-    burst = serve(args.lanes, 64, False)
-    print(f"serve: burst {burst}", file=sys.stderr, flush=True)
-    single = serve(1, 1, False)
+    burst = single = None
+    if args.serve_burst:
+        burst = serve(args.lanes, 64, False)
+        print(f"serve: burst {burst}", file=sys.stderr, flush=True)
+        single = serve(1, 1, False)
     line = {"metric": f"served queries/s at Poisson {args.rate:g}/s offered (p50/p99 latency beside)",
             "value": poisson["queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": 1, "warmup": 0,
             "ms_per_step": poisson["wall_s"] * 1000, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": f"{len(graphs)} resident RMAT graphs (scales {scales}, edge factor 16), "
-                                   f"{nq} queries, uniform graph x 64 mixed patterns",
+            "config": {"workload": f"{len(gids)} resident RMAT graphs (scales {scales}, edge factor 16), "
+                                   f"{nq} queries, uniform graph x {len(pats)} mixed patterns (of 64 drawn, "
+                                   "without general cores and fringed-centre wedges)",
+                       "graphs": [{"scale": sc, "n": n, "m_directed": m} for sc, (n, m) in zip(scales, graph_sizes)],
+                       "distinct_queries": len(direct),
                        "lanes": args.lanes, "budget_gb": args.budget_gb, "gen_s": round(gen_s, 1)},
             "p50_ms": poisson["p50_ms"], "p99_ms": poisson["p99_ms"], "poisson": poisson,
             "burst_batched": burst, "burst_one_query_per_launch": single,
-            "batched_over_single": burst["queries_per_s"] / max(single["queries_per_s"], 1e-12),
+            "batched_over_single": (burst["queries_per_s"] / max(single["queries_per_s"], 1e-12)) if burst else None,
             "gpu_launches": launches, "exact": "every served count equals the direct count"}
     print(json.dumps(line))
     ctx.close()
@@ -751,15 +796,21 @@ def main():
                          "one graph; packed: batching across graphs; serve: the serving loop")
     ap.add_argument("--mixed-patterns", type=int, default=64, help="mixed: patterns drawn")
     ap.add_argument("--mixed-scale", type=int, default=24, help="mixed: RMAT scale for cores of <= 3 vertices")
-    ap.add_argument("--general-scale", type=int, default=12,
+    ap.add_argument("--general-scale", type=int, default=6,
                     help="mixed: RMAT scale for general cores and fringed-centre wedges")
+    ap.add_argument("--general-budget", type=float, default=300.0,
+                    help="mixed: seconds of single counts on the general-core graph; patterns beyond it are "
+                         "listed, not timed")
     ap.add_argument("--graphs", type=int, default=256, help="packed: member graphs")
     ap.add_argument("--nmax", type=int, default=50000, help="packed: largest member size")
     ap.add_argument("--serve-scales", default="6,7,8,9,10,11,12,13", help="serve: RMAT scales")
     ap.add_argument("--queries", type=int, default=300, help="serve: queries")
     ap.add_argument("--rate", type=float, default=5.0, help="serve: Poisson arrivals per second")
     ap.add_argument("--lanes", type=int, default=4, help="serve: lanes")
-    ap.add_argument("--budget-gb", type=float, default=150.0, help="serve: work-arena budget")
+    ap.add_argument("--budget-gb", type=float, default=150.0,
+                    help="serve: memory budget (registered graphs and work arenas)")
+    ap.add_argument("--serve-burst", type=int, default=1,
+                    help="serve: also run the queries as a burst, batched and one per launch")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
