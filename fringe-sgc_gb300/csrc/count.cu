@@ -281,6 +281,7 @@ struct TriParams {
   int relabel;  // roles by (deg, id) order (1) or by id (0)
   int kmax;     // largest out-degree (bitmap kernel)
   int stage;    // bitmap kernel: longest N(a) staged in shared memory (ints, multiple of 32)
+  int row_words;  // bitmap kernel: a vertex's rows are kept in shared memory up to this many words
   int walk_ratio;  // bitmap kernel: walk N(b) when deg b <= walk_ratio * deg a
   Rot3 rot;
 };
@@ -471,13 +472,14 @@ __global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g
   __shared__ int s_a;
   __shared__ __align__(8) unsigned long long s_bar;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  unsigned* bits = bits_all + (size_t)blockIdx.x * (size_t)bits_per_block;
+  unsigned* const gbits = bits_all + (size_t)blockIdx.x * (size_t)bits_per_block;
   const int kmax = p.kmax, stage = p.stage;
   int* s_na = s_dyn;                              // staged N(a): stage + 4 ints (16-byte aligned)
   unsigned* s_row = reinterpret_cast<unsigned*>(s_dyn + stage + 4);  // per warp: stage / 32 words
   int* outl = s_dyn + stage + 4 + (stage >> 5) * (kTriThreads >> 5);  // out-neighbours of a
   int* pos = outl + kmax;                         // their positions in N(a)
   int* rowpop = outl + 2 * kmax;                  // |N(a) & N(b_i)|
+  unsigned* s_bits = reinterpret_cast<unsigned*>(outl + 3 * kmax);  // rows of small vertices: p.row_words
   unsigned parity = 0;
   if (threadIdx.x == 0 && stage > 0) mbar_init(&s_bar, 1);
   __syncthreads();
@@ -494,6 +496,8 @@ __global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g
     const int da = g.deg[a];
     if (k >= 2 && da >= p.sum1) {
       const int W = (da + 31) >> 5;
+      // the rows stay in shared memory when they fit, else in the global arena
+      unsigned* const bits = ((long long)k * W <= p.row_words) ? s_bits : gbits;
       const long long abeg = g.off[a];
       const bool staged = da <= stage;
       const int* Na = g.adj + abeg;
@@ -1136,6 +1140,7 @@ struct GenParams {
   uint8_t list[5];
   int nslots;
   int lane_venn_max;  // a lane builds its own match's Venn row up to this many list entries
+  int grab;           // list entries a warp takes from the queue at a time (1..32)
   uint8_t slot_idx[kMaxSlots];  // region bitmap of each placement step
   uint8_t slot_set[kMaxSlots];  // anchor set index of each step
   uint8_t slot_top[kMaxSlots];  // 1 if the step takes all remaining fringes
@@ -1407,10 +1412,11 @@ __device__ A gen_level(const GView& g, const GenParams& p, GenWarp& w) {
 
 // One warp per directed edge (u, v) at a time, u = core vertex A and v = core
 // vertex B (the reference's worklist of general_core_level0,
-// src/fringeCount.cu:567-663, with its degree pruning): warps take 32
-// consecutive list entries from a queue, find their owners in parallel and
-// then walk each entry's matches.  Work is spread per edge, so a hub's edges
-// go to many warps.
+// src/fringeCount.cu:567-663, with its degree pruning): warps take p.grab
+// (1..32) consecutive list entries from a queue, find their owners in
+// parallel and then walk each entry's matches.  Work is spread per edge, so a
+// hub's edges go to many warps; on small graphs a warp takes one edge at a
+// time, so that every warp of the GPU has work.
 template <int D, class A>
 __global__ void __launch_bounds__(kGenWarps * 32) general_core_kernel(GView g, const __grid_constant__ GenParams p,
                                                                        unsigned long long* __restrict__ queue,
@@ -1422,11 +1428,11 @@ __global__ void __launch_bounds__(kGenWarps * 32) general_core_kernel(GView g, c
   const unsigned long long m = (unsigned long long)g.m;
   for (;;) {
     unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(queue, 32ULL);
+    if (lane == 0) base = atomicAdd(queue, (unsigned long long)p.grab);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= m) break;
     const long long j = (long long)base + lane;
-    bool ok = j < (long long)m;
+    bool ok = lane < p.grab && j < (long long)m;
     int u = 0, v = 0;
     if (ok) {
       int lo = 0, hi = g.n;  // owner: the last vertex with off[u] <= j
@@ -1564,13 +1570,21 @@ bool triangle_uses_bitmaps(const fsgc_matching_order&, const DevGraph& G, int mo
 // long an N(a) stage as fits a 72 KB block (three blocks per SM): 4 bytes per
 // staged entry plus one row bit per warp.  Returns the stage length (a multiple
 // of 32, or 0) and the block's dynamic shared memory.
-int triangle_stage(int kmax, int stage_max, size_t* smem) {
+// Bitmap kernel shared memory (a 72 KB block, three per SM): the out-neighbour
+// arrays (3 ints each), the N(a) stage (4 bytes per staged entry plus one row
+// bit per warp) up to stage_max entries, and whatever remains for the rows of
+// vertices small enough to keep them in shared memory.  Returns the stage
+// length (a multiple of 32, or 0); *row_words and *smem are set.
+int triangle_stage(int kmax, int stage_max, int* row_words, size_t* smem) {
   const long long fixed = 3LL * 4 * std::max(1, kmax);
   const long long budget = 72LL * 1024 - fixed - 16;
   long long stage = budget > 0 ? budget / (4 + (kTriThreads / 32) * 4 / 32) : 0;
   stage = std::min<long long>(stage, std::min(8192, std::max(0, stage_max))) & ~31LL;
   if (stage < 64) stage = 0;
-  *smem = (size_t)(4 * (stage + 4) + 4 * (stage / 32) * (kTriThreads / 32) + fixed);
+  const long long used = 4 * (stage + 4) + 4 * (stage / 32) * (kTriThreads / 32) + fixed;
+  const long long rows = std::max(0LL, (72LL * 1024 - used) / 4);
+  *row_words = (int)rows;
+  *smem = (size_t)(used + 4 * rows);
   return (int)stage;
 }
 
@@ -1714,7 +1728,7 @@ int launch_triangle_set(DevGraph& G, const GView& gv, TriParams tp, const TriSet
                         uint64_t* launches, DevWork& work) {
   size_t smem = 0;
   tp.kmax = (int)G.max_outdeg;
-  tp.stage = triangle_stage(tp.kmax, work.tune.triangle_stage_max, &smem);
+  tp.stage = triangle_stage(tp.kmax, work.tune.triangle_stage_max, &tp.row_words, &smem);
   tp.walk_ratio = std::max(0, work.tune.triangle_walk_ratio);
   long long per_block;
   int blocks;
@@ -1905,6 +1919,8 @@ int enqueue_count_a(CountJob& job, cudaStream_t s, uint64_t* launches, DevWork& 
   auto* queue = reinterpret_cast<unsigned long long*>(work.small + 5);
   cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
   const int blocks = sm_count() * std::min(16, std::max(1, work.tune.general_blocks_per_sm));
+  // one edge per grab until there are many more edges than warps
+  gp->grab = (int)std::max(1LL, std::min(32LL, G.m / ((long long)blocks * kGenWarps * 64)));
   // the placement walk's state is sized by the step count
   if (ns <= 32) general_core_kernel<32, A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
   else if (ns <= 64) general_core_kernel<64, A><<<blocks, kGenWarps * 32, 0, s>>>(gv, *gp, queue, job.d_slot);
