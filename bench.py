@@ -511,8 +511,9 @@ def run_mixed(args):
     carries fringes: per_match_family) have work that grows by one to two
     orders of magnitude per two RMAT scales, so they run on the RMAT graph of
     scale --general-scale, with the same two modes, cheapest first by their
-    fringe-placement bound, within --general-budget seconds of single counts;
-    the rest are listed, not timed (a general core enumerates every fringe
+    fringe-placement bound, within --general-budget seconds of single counts
+    (the others within --mixed-budget seconds on the main graph, in the same
+    order); the rest are listed, not timed (a general core enumerates every fringe
     placement of every core match, and for drawn patterns with many anchor
     sets that is billions of steps even on a 64-vertex graph).  Every batched
     count equals its single count."""
@@ -539,8 +540,10 @@ def run_mixed(args):
                 if time.time() - t0 > budget_s:
                     not_timed.append(name)
                     continue
+                t1 = time.time()
                 ctx.count(gid, mo)
                 kept.append((name, mo))
+                print(f"mixed: RMAT-{scale} {name} {time.time() - t1:.2f} s", file=sys.stderr, flush=True)
             group = kept
         mos = [mo for _, mo in group]
         single = [ctx.count(gid, mo) for mo in mos]  # also builds every per-graph structure
@@ -569,7 +572,7 @@ def run_mixed(args):
                 "not_timed": not_timed}
 
     launches0 = ctx.launches
-    main_part = measure(args.mixed_scale, small)
+    main_part = measure(args.mixed_scale, small, args.mixed_budget)
     gen_part = measure(args.general_scale, general, args.general_budget) if general else None
     line = {"metric": "queries/s, mixed patterns on one graph (batched in shared passes from a captured CUDA graph)",
             "value": main_part["batched_queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
@@ -801,6 +804,9 @@ def main():
     ap.add_argument("--general-budget", type=float, default=300.0,
                     help="mixed: seconds of single counts on the general-core graph; patterns beyond it are "
                          "listed, not timed")
+    ap.add_argument("--mixed-budget", type=float, default=600.0,
+                    help="mixed: seconds of single counts on the main graph; patterns beyond it are listed, "
+                         "not timed")
     ap.add_argument("--graphs", type=int, default=256, help="packed: member graphs")
     ap.add_argument("--nmax", type=int, default=50000, help="packed: largest member size")
     ap.add_argument("--serve-scales", default="6,7,8,9,10,11,12,13", help="serve: RMAT scales")

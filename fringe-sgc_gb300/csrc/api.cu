@@ -1198,6 +1198,35 @@ void fsgc_x128_host(int op, unsigned long long a_lo, unsigned long long a_hi, un
   out[2] = r.is_saturated() ? 1 : 0;
 }
 
+// Host evaluation of the wedge-pair formula (the same __host__ __device__
+// code as the kernels) with the general binomials (k01 = 0) or the k <= 1
+// form the kernels take when every fringe count is 0 or 1 (k01 = 1), in u64
+// (exact = 0) or exact 128-bit arithmetic (exact = 1).  out = (lo, hi).
+void fsgc_wedge_formula_host(int dx, int dy, int adj, int f_x, int f_xy, int f_y, int c, int k01, int exact,
+                             unsigned long long* out) {
+  static fsgc::DivMagic tab[fsgc::kMaxDiv];
+  static bool init = false;
+  if (!init) {
+    for (int d = 2; d < fsgc::kMaxDiv; d++) tab[d] = fsgc::make_div_magic((unsigned)d);
+    init = true;
+  }
+  if (exact) {
+    const fsgc::X128 r =
+        k01 ? fsgc::wedge_formula_with<fsgc::X128>(dx, dy, adj != 0, f_x, f_xy, f_y, c,
+                                                   [](int n, int k) { return fsgc::X128(fsgc::nck01(n, k)); })
+            : fsgc::wedge_formula_with<fsgc::X128>(dx, dy, adj != 0, f_x, f_xy, f_y, c,
+                                                   [](int n, int k) { return fsgc::nck_x(n, k); });
+    out[0] = r.lo;
+    out[1] = r.hi;
+  } else {
+    out[0] = k01 ? fsgc::wedge_formula_with<uint64_t>(dx, dy, adj != 0, f_x, f_xy, f_y, c,
+                                                      [](int n, int k) { return (uint64_t)fsgc::nck01(n, k); })
+                 : fsgc::wedge_formula_with<uint64_t>(dx, dy, adj != 0, f_x, f_xy, f_y, c,
+                                                      [](int n, int k) { return (uint64_t)fsgc::nck_ref(n, k, tab); });
+    out[1] = 0;
+  }
+}
+
 unsigned long long fsgc_div_small_host(unsigned long long x, unsigned d) {
   if (d < 2 || d >= (unsigned)fsgc::kMaxDiv) return 0;
   return fsgc::div_magic(x, fsgc::make_div_magic(d));

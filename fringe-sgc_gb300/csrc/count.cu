@@ -84,23 +84,22 @@ __device__ A edge_formula(int du, int dv, int c_uv, int f_u, int f_uv, int f_v) 
   return acc * nck_a<A>(c_uv, f_uv);
 }
 
-// wedge() (src/fringeCount.cu:1381-1406): endpoints x (larger id) and y of a
-// wedge; c = common neighbours of x and y other than the centre.
+// Binomials for wedge_formula_with: the count's arithmetic in general, and
+// the two-case form when every k is 0 or 1 (nck01, equal for those k).
 template <class A>
-__device__ A wedge_formula(int dx, int dy, bool adj, int f_x, int f_xy, int f_y, int c) {
-  const int a_xy = c - f_xy;
-  if (a_xy < 0) return 0;
-  const int corr = adj ? 2 : 1;
-  const int a_x = dx - (corr + c), a_y = dy - (corr + c);
-  const int bound = min(f_x, a_xy);
-  A sum = 0;
-  for (int j = 0; j <= bound; j++) {
-    const int k = f_x - j;
-    A term = nck_a<A>(a_x, k) * nck_a<A>(a_xy + a_y - j, f_y);
-    if (f_x != f_y) term += nck_a<A>(a_y, k) * nck_a<A>(a_xy + a_x - j, f_y);
-    sum += term * nck_a<A>(a_xy, j);
-  }
-  return sum * nck_a<A>(c, f_xy);
+struct NckA {
+  __device__ A operator()(int n, int k) const { return nck_a<A>(n, k); }
+};
+template <class A>
+struct Nck01 {
+  __device__ A operator()(int n, int k) const { return A(nck01(n, k)); }
+};
+
+// wedge() (src/fringeCount.cu:1381-1406) for endpoints x (larger id) and y.
+template <class A>
+__device__ __forceinline__ A wedge_formula(int dx, int dy, bool adj, int f_x, int f_xy, int f_y, int c) {
+  if ((unsigned)(f_x | f_xy | f_y) <= 1u) return wedge_formula_with<A>(dx, dy, adj, f_x, f_xy, f_y, c, Nck01<A>());
+  return wedge_formula_with<A>(dx, dy, adj, f_x, f_xy, f_y, c, NckA<A>());
 }
 
 // fc3 (src/fringeCount.cu:233-327): placements of the seven anchor-set types of
@@ -281,7 +280,6 @@ struct TriParams {
   int relabel;  // roles by (deg, id) order (1) or by id (0)
   int kmax;     // largest out-degree (bitmap kernel)
   int stage;    // bitmap kernel: longest N(a) staged in shared memory (ints, multiple of 32)
-  int row_words;  // bitmap kernel: a vertex's rows are kept in shared memory up to this many words
   int walk_ratio;  // bitmap kernel: walk N(b) when deg b <= walk_ratio * deg a
   Rot3 rot;
 };
@@ -472,14 +470,13 @@ __global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g
   __shared__ int s_a;
   __shared__ __align__(8) unsigned long long s_bar;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  unsigned* const gbits = bits_all + (size_t)blockIdx.x * (size_t)bits_per_block;
+  unsigned* bits = bits_all + (size_t)blockIdx.x * (size_t)bits_per_block;
   const int kmax = p.kmax, stage = p.stage;
   int* s_na = s_dyn;                              // staged N(a): stage + 4 ints (16-byte aligned)
   unsigned* s_row = reinterpret_cast<unsigned*>(s_dyn + stage + 4);  // per warp: stage / 32 words
   int* outl = s_dyn + stage + 4 + (stage >> 5) * (kTriThreads >> 5);  // out-neighbours of a
   int* pos = outl + kmax;                         // their positions in N(a)
   int* rowpop = outl + 2 * kmax;                  // |N(a) & N(b_i)|
-  unsigned* s_bits = reinterpret_cast<unsigned*>(outl + 3 * kmax);  // rows of small vertices: p.row_words
   unsigned parity = 0;
   if (threadIdx.x == 0 && stage > 0) mbar_init(&s_bar, 1);
   __syncthreads();
@@ -496,8 +493,6 @@ __global__ void __launch_bounds__(kTriThreads, 3) triangle_bitmap_kernel(GView g
     const int da = g.deg[a];
     if (k >= 2 && da >= p.sum1) {
       const int W = (da + 31) >> 5;
-      // the rows stay in shared memory when they fit, else in the global arena
-      unsigned* const bits = ((long long)k * W <= p.row_words) ? s_bits : gbits;
       const long long abeg = g.off[a];
       const bool staged = da <= stage;
       const int* Na = g.adj + abeg;
@@ -697,6 +692,26 @@ __device__ __forceinline__ int nth_set_bit(unsigned mask, int n) {
 __device__ __forceinline__ int wedge_counter_bits(int dv) { return dv <= 15 ? 4 : (dv <= 255 ? 8 : 16); }
 static_assert(WedgeCfg<false>::TW == kWThreads && WedgeCfg<true>::TW == kWThreads, "one bitmap word per thread");
 
+// One non-zero counter handed from the counter words to the evaluation: its
+// offset o in the chunk and its centre count C.  SMALL: o < 2^18 and
+// C <= kWDvMax pack into 32 bits; BIG: 32-bit counts take 64.
+template <bool BIG>
+struct WedgePair {
+  using T = unsigned;
+  __device__ static T pack(int o, unsigned c) { return ((unsigned)o << 12) | c; }
+  __device__ static int off(T x) { return (int)(x >> 12); }
+  __device__ static unsigned count(T x) { return x & 0xfffu; }
+};
+template <>
+struct WedgePair<true> {
+  using T = unsigned long long;
+  __device__ static T pack(int o, unsigned c) { return ((unsigned long long)o << 32) | c; }
+  __device__ static int off(T x) { return (int)(x >> 32); }
+  __device__ static unsigned count(T x) { return (unsigned)x; }
+};
+static_assert(kWDvMax < 4096 && WedgeCfg<false>::CH_MAX <= (1 << 20), "SMALL pairs pack into 32 bits");
+constexpr int kPairBuf = 128;  // pairs staged per warp and pass
+
 template <bool BIG>
 struct WedgeSmem {
   unsigned cnt[WedgeCfg<BIG>::WORDS];
@@ -705,11 +720,16 @@ struct WedgeSmem {
   unsigned adjbits[WedgeCfg<BIG>::CH_MAX / 32];
   long long cur[BIG ? 1 : kWDvMax];
   long long lim[BIG ? 1 : kWDvMax];
+  typename WedgePair<BIG>::T pairs[kWThreads / 32][kPairBuf];
   int pre[BIG ? 1 : kWDvMax + 1];
   int warp_tmp[33];
   int v;
   int lo;
+  int grab;  // next touched word to evaluate
 };
+// dynamic shared memory of one block, with 1 KB left for the reductions' static arrays
+static_assert(sizeof(WedgeSmem<false>) + 1024 <= 232448 && sizeof(WedgeSmem<true>) + 1024 <= 232448,
+              "wedge kernel shared memory");
 
 // Per high-degree vertex u: offsets in N(u) of the first neighbour >= k *
 // kWGran, for every k.  A chunk that ends on such a boundary finds the end of
@@ -895,11 +915,12 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
         }
       }
       __syncthreads();
-      // evaluate: the chunk's touched counter words are split evenly over the
-      // warps (a prefix over the touched-bitmap words); a warp loads 32 words
-      // at a time, one per lane, prefix-sums their non-zero counters and then
-      // hands out one (endpoint, centre count) pair per lane per step, so the
-      // lanes evaluate in lockstep and adjacent lanes take adjacent endpoints.
+      // evaluate: the chunk's touched counter words are numbered by a prefix
+      // over the touched-bitmap words; a warp takes 32 words at a time, one
+      // per lane, prefix-sums their non-zero counters, writes
+      // them as (offset, centre count) pairs into its shared-memory buffer and
+      // then evaluates one pair per lane per step, so the lanes evaluate in
+      // lockstep and adjacent lanes take adjacent endpoints.
       {
         const int nw = (hi - lo + (1 << lper) - 1) >> lper;
         const int ntw = (nw + 31) >> 5;
@@ -924,11 +945,20 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
         __syncthreads();
         S.tpre[tid] = S.warp_tmp[warp] + inc - c0;
         const int T = S.warp_tmp[32];
+        if (tid == 0) S.grab = 0;
         __syncthreads();
-        const int W0 = (int)(((long long)T * warp) / nwarp), W1 = (int)(((long long)T * (warp + 1)) / nwarp);
         const int lbits = BIG ? 5 : (lper == 1 ? 4 : (lper == 2 ? 3 : 2));  // log2(bits)
         const unsigned cmask = BIG ? 0xffffffffu : ((1u << bits) - 1);
-        for (int W = W0; W < W1; W += 32) {
+        using PT = WedgePair<BIG>;
+        typename PT::T* buf = S.pairs[warp];
+        // warps take the touched words 32 at a time from a shared counter, so
+        // a warp whose words hold more pairs takes fewer of them
+        for (;;) {
+          int W = 0;
+          if (lane == 0) W = atomicAdd(&S.grab, 32);
+          W = __shfl_sync(0xffffffffu, W, 0);
+          if (W >= T) break;
+          const int W1 = min(W + 32, T);
           const int idx = W + lane;
           int wd = 0, c = 0;
           unsigned word = 0, nz = 0;
@@ -951,23 +981,24 @@ __global__ void __launch_bounds__(kWThreads, 1) wedge_chunk_kernel(GView g, Wedg
           }
           const int excl = incl - c;
           const int P = __shfl_sync(0xffffffffu, incl, 31);
-          for (int q = 0; q < P; q += 32) {
-            const int i = q + lane;
-            int s = 0;  // source lane: the last with excl <= i
-            for (int step = 16; step >= 1; step >>= 1) {
-              const int e = __shfl_sync(0xffffffffu, excl, s + step);
-              if (e <= i) s += step;
+          // pairs excl .. excl + c - 1 are this lane's; a pass stages the
+          // pairs [base, base + kPairBuf) and evaluates them
+          for (int base = 0; base < P; base += kPairBuf) {
+            unsigned mk = nz;
+            for (int t = 0; t < c; t++) {
+              const int kbit = __ffs(mk) - 1;  // low bit of the counter
+              mk &= mk - 1;
+              const int pos = excl + t - base;
+              if (pos >= 0 && pos < kPairBuf) buf[pos] = PT::pack((wd << lper) + (kbit >> lbits), (word >> kbit) & cmask);
             }
-            const int wdS = __shfl_sync(0xffffffffu, wd, s);
-            const unsigned wordS = __shfl_sync(0xffffffffu, word, s);
-            const unsigned nzS = __shfl_sync(0xffffffffu, nz, s);
-            const int exS = __shfl_sync(0xffffffffu, excl, s);
-            if (i < P) {
-              const int kbit = nth_set_bit(nzS, i - exS);  // low bit of the counter
-              const unsigned C = (wordS >> kbit) & cmask;
-              const int o = (wdS << lper) + (kbit >> lbits);
-              eval_pair<BIG, NP, A>(g, ws, S, o, C, g.deg[lo + o], v, dv, acc);
+            __syncwarp();
+            const int np = min(kPairBuf, P - base);
+            for (int i = lane; i < np; i += 32) {
+              const typename PT::T x = buf[i];
+              const int o = PT::off(x);
+              eval_pair<BIG, NP, A>(g, ws, S, o, PT::count(x), __ldg(g.deg + lo + o), v, dv, acc);
             }
+            __syncwarp();
           }
         }
       }
@@ -1568,23 +1599,19 @@ bool triangle_uses_bitmaps(const fsgc_matching_order&, const DevGraph& G, int mo
 
 // Bitmap kernel shared memory: the out-neighbour arrays (3 ints each), then as
 // long an N(a) stage as fits a 72 KB block (three blocks per SM): 4 bytes per
-// staged entry plus one row bit per warp.  Returns the stage length (a multiple
-// of 32, or 0) and the block's dynamic shared memory.
-// Bitmap kernel shared memory (a 72 KB block, three per SM): the out-neighbour
-// arrays (3 ints each), the N(a) stage (4 bytes per staged entry plus one row
-// bit per warp) up to stage_max entries, and whatever remains for the rows of
-// vertices small enough to keep them in shared memory.  Returns the stage
-// length (a multiple of 32, or 0); *row_words and *smem are set.
-int triangle_stage(int kmax, int stage_max, int* row_words, size_t* smem) {
+// staged entry plus one row bit per warp, up to stage_max entries.  Returns the
+// stage length (a multiple of 32, or 0) and the block's dynamic shared memory.
+// The bitmap rows stay in the global arena: keeping the rows of small vertices
+// in a full 72 KB block made the 4-clique pattern of the RMAT-22 benchmark 58%
+// slower, most likely because the larger shared-memory carve-out leaves the
+// kernel's list reads a small L1.
+int triangle_stage(int kmax, int stage_max, size_t* smem) {
   const long long fixed = 3LL * 4 * std::max(1, kmax);
   const long long budget = 72LL * 1024 - fixed - 16;
   long long stage = budget > 0 ? budget / (4 + (kTriThreads / 32) * 4 / 32) : 0;
   stage = std::min<long long>(stage, std::min(8192, std::max(0, stage_max))) & ~31LL;
   if (stage < 64) stage = 0;
-  const long long used = 4 * (stage + 4) + 4 * (stage / 32) * (kTriThreads / 32) + fixed;
-  const long long rows = std::max(0LL, (72LL * 1024 - used) / 4);
-  *row_words = (int)rows;
-  *smem = (size_t)(used + 4 * rows);
+  *smem = (size_t)(4 * (stage + 4) + 4 * (stage / 32) * (kTriThreads / 32) + fixed);
   return (int)stage;
 }
 
@@ -1728,7 +1755,7 @@ int launch_triangle_set(DevGraph& G, const GView& gv, TriParams tp, const TriSet
                         uint64_t* launches, DevWork& work) {
   size_t smem = 0;
   tp.kmax = (int)G.max_outdeg;
-  tp.stage = triangle_stage(tp.kmax, work.tune.triangle_stage_max, &tp.row_words, &smem);
+  tp.stage = triangle_stage(tp.kmax, work.tune.triangle_stage_max, &smem);
   tp.walk_ratio = std::max(0, work.tune.triangle_walk_ratio);
   long long per_block;
   int blocks;

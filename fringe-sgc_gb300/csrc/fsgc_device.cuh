@@ -64,6 +64,32 @@ __host__ __device__ inline u64 nck_ref(int n, int k, const DivMagic* tab) {
   return r;
 }
 
+// C(n, k) for k = 0 or 1, equal to nck_ref(n, k) (and to the exact C(n, k))
+// for every n: 1 if n >= 0 when k = 0; n if n >= 1 when k = 1; 0 otherwise.
+__host__ __device__ inline u64 nck01(int n, int k) {
+  return k == 0 ? (n >= 0 ? 1ULL : 0ULL) : (n >= 1 ? (u64)n : 0ULL);
+}
+
+// wedge() (src/fringeCount.cu:1381-1406): endpoints x (larger id) and y of a
+// wedge; c = common neighbours of x and y other than the centre.  `nk(n, k)`
+// gives the binomials in the count's arithmetic A.
+template <class A, class Nck>
+__host__ __device__ inline A wedge_formula_with(int dx, int dy, bool adj, int f_x, int f_xy, int f_y, int c, Nck nk) {
+  const int a_xy = c - f_xy;
+  if (a_xy < 0) return A(0);
+  const int corr = adj ? 2 : 1;
+  const int a_x = dx - (corr + c), a_y = dy - (corr + c);
+  const int bound = (f_x < a_xy) ? f_x : a_xy;
+  A sum = A(0);
+  for (int j = 0; j <= bound; j++) {
+    const int k = f_x - j;
+    A term = nk(a_x, k) * nk(a_xy + a_y - j, f_y);
+    if (f_x != f_y) term += nk(a_y, k) * nk(a_xy + a_x - j, f_y);
+    sum += term * nk(a_xy, j);
+  }
+  return sum * nk(c, f_xy);
+}
+
 // ----------------------------------------------------------------------------
 // Sorted-list helpers.  Lists are ascending int32 runs in global memory (the
 // read-only loads below take global addresses only).

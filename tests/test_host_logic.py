@@ -52,6 +52,58 @@ def test_x128_binomial_like_python():
         assert (sat, v) == ((True, M128) if want >= M128 else (False, want)), (n, k)
 
 
+def wedge_formula(dx, dy, adj, fx, fxy, fy, c, k01, exact):
+    L = fsgc.lib()
+    L.fsgc_wedge_formula_host.restype = None
+    L.fsgc_wedge_formula_host.argtypes = [C.c_int] * 9 + [C.POINTER(C.c_ulonglong)]
+    out = (C.c_ulonglong * 2)()
+    L.fsgc_wedge_formula_host(dx, dy, adj, fx, fxy, fy, c, k01, exact, out)
+    return out[0] | (out[1] << 64)
+
+
+def wedge_formula_python(dx, dy, adj, fx, fxy, fy, c):
+    """wedge() of the reference (src/fringeCount.cu:1381-1406) in Python
+    integers, binomials 0 outside 0 <= k <= n."""
+    def comb(n, k):
+        return math.comb(n, k) if 0 <= k <= n else 0
+    a_xy = c - fxy
+    if a_xy < 0:
+        return 0
+    corr = 2 if adj else 1
+    a_x, a_y = dx - (corr + c), dy - (corr + c)
+    s = 0
+    for j in range(min(fx, a_xy) + 1):
+        k = fx - j
+        t = comb(a_x, k) * comb(a_xy + a_y - j, fy)
+        if fx != fy:
+            t += comb(a_y, k) * comb(a_xy + a_x - j, fy)
+        s += t * comb(a_xy, j)
+    return s * comb(c, fxy)
+
+
+def test_wedge_formula_k01_form_equals_general_binomials():
+    """The kernels evaluate wedge() with two-case binomials when every fringe
+    count is 0 or 1; that must give the general form's value bit for bit,
+    including where the u64 products wrap and for arguments outside the
+    kernels' range (negative Venn sizes)."""
+    rng = random.Random(11)
+    cases = [(dx, dy, adj, c) for dx in range(0, 9) for dy in range(0, 9) for adj in (0, 1) for c in range(-2, 8)]
+    for _ in range(3000):
+        big = rng.choice([100, 70000, 2**20, 2**31 - 1])
+        c = rng.randrange(0, min(big, 3000))
+        cases.append((rng.randrange(c, big), rng.randrange(c, big), rng.randrange(2), c))
+    for fx in (0, 1):
+        for fxy in (0, 1):
+            for fy in (0, 1):
+                for dx, dy, adj, c in cases:
+                    u = wedge_formula(dx, dy, adj, fx, fxy, fy, c, 0, 0)
+                    assert wedge_formula(dx, dy, adj, fx, fxy, fy, c, 1, 0) == u, (dx, dy, adj, fx, fxy, fy, c)
+                    x = wedge_formula(dx, dy, adj, fx, fxy, fy, c, 1, 1)
+                    assert wedge_formula(dx, dy, adj, fx, fxy, fy, c, 0, 1) == x
+                    want = wedge_formula_python(dx, dy, adj, fx, fxy, fy, c)
+                    assert x == min(want, M128) and u == want % 2**64, (dx, dy, adj, fx, fxy, fy, c)
+
+
 def test_entry_points_reject_null_arguments():
     L = fsgc.lib()
     p = C.c_void_p()
