@@ -106,3 +106,67 @@ def test_random_patterns_against_the_reference_decomposer(tmp_path):
             assert fsgc.preprocess(n, edges).to_bytes().hex() == want, (i, n, edges)
             checked += 1
     assert checked > 200 and rejected > 0  # dense draws often need a core above six vertices
+
+
+def test_ten_thousand_mixed_draws_against_the_reference_decomposer(tmp_path):
+    """Where the reference's own fringePreprocess is built: 10,000 seeded
+    patterns drawn as the mixed-pattern workloads draw them (a core from edge,
+    wedge, triangle, 4-path, 4-cycle, diamond, 4-clique, 5-cycle; 0-12 fringe
+    vertices, each joined to a uniformly random nonempty subset of the core),
+    with the vertex ids shuffled, decompose to the same defined bytes or are
+    rejected by both."""
+    import concurrent.futures as cf
+    import random
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, os.path.join(root, "tests", "golden"))
+    sys.path.insert(0, root)
+    import oracle
+    from bench import CORE_SHAPES
+    from make_golden import defined_bytes
+    if not os.path.exists(oracle.REF_PREPROCESS):
+        pytest.skip("the reference's fringePreprocess is not built here")
+    rng = random.Random(20251209)
+    shapes = sorted(CORE_SHAPES)
+    draws = []
+    for _ in range(10000):
+        k, core = CORE_SHAPES[rng.choice(shapes)]
+        nf = rng.randint(0, 12)
+        edges = list(core)
+        for i in range(nf):
+            sub = rng.randrange(1, 1 << k)
+            edges += [(j, k + i) for j in range(k) if sub >> j & 1]
+        n = k + nf
+        perm = list(range(n))
+        rng.shuffle(perm)
+        draws.append((n, sorted((min(perm[a], perm[b]), max(perm[a], perm[b])) for a, b in edges)))
+
+    def reference(job):
+        worker, chunk = job
+        wd = tmp_path / f"w{worker}"
+        wd.mkdir()
+        out = []
+        for n, edges in chunk:
+            try:
+                out.append(defined_bytes(oracle.reference_preprocess([n] + [x for e in edges for x in e], str(wd))).hex())
+            except RuntimeError:
+                out.append(None)
+        return out
+
+    workers = 8
+    jobs = [(w, draws[w::workers]) for w in range(workers)]
+    with cf.ThreadPoolExecutor(workers) as ex:
+        parts = list(ex.map(reference, jobs))
+    want = [None] * len(draws)
+    for w, part in enumerate(parts):
+        want[w::workers] = part
+    checked = rejected = 0
+    for i, ((n, edges), ref) in enumerate(zip(draws, want)):
+        if ref is None:
+            with pytest.raises(fsgc.FsgcError):
+                fsgc.preprocess(n, edges)
+            rejected += 1
+        else:
+            assert fsgc.preprocess(n, edges).to_bytes().hex() == ref, (i, n, edges)
+            checked += 1
+    assert checked + rejected == 10000 and checked > 5000
