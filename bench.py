@@ -891,6 +891,9 @@ def main():
                    "n": g.n, "m_directed": g.m, "max_degree": out["graph"]["max_degree"],
                    "patterns": list(WORKLOAD), "parallelism": f"replicas x{world}",
                    "l2": "inputs (0.5 GB CSR) larger than L2, and L2 flushed before every timed step",
+                   "divisor": "each pattern's divisor (the pattern counted in itself, on its own graph of 4-12 "
+                              "vertices) is computed at the first count and cached, so the timed steps leave it "
+                              "out; the reference's runtime: line includes it",
                    "prep_ms": round(out["prep_ms"], 3),
                    "per_pattern_ms": {k: round(v, 3) for k, v in out["per_task_ms"].items()},
                    "edges_per_s": {k: (round(v, 1) if v is not None else None)

@@ -449,9 +449,10 @@ __global__ void triangle_core_kernel(GView g, TriParams p, u64* __restrict__ slo
 constexpr int kTriThreads = 256;
 constexpr int kBulkWaitPolls = 1 << 22;  // bounded wait for a bulk copy
 
-// Triangle-core patterns counted together: the bitmaps, roles and Venn sizes
-// of a triangle do not depend on the pattern, only the pruning thresholds and
-// the placement formulas do.  p.sum1 (the vertex gate) is the set's smallest.
+// Triangle-core patterns of one pass: the bitmaps, roles and Venn sizes of a
+// triangle do not depend on the pattern, only the pruning thresholds and the
+// placement formulas do.  p.sum1 (the vertex gate) is the set's smallest.
+// Every launch today carries one pattern (see enqueue_count_set).
 constexpr int kTriFuse = 4;
 struct TriSet {
   int np;
@@ -2089,20 +2090,19 @@ int enqueue_count_set(std::vector<CountJob*>& jobs, cudaStream_t s, uint64_t* la
                     : launch_wedge_set<kWedgeFuse, u64>(G, gv, ws, s, launches, work);
     if (st != FSGC_OK) return st;
   }
-  for (size_t b = 0; b < tris.size(); b += kTriFuse) {
+  // Triangle-core patterns get one bitmap pass each.  A pass over four
+  // patterns shares the row build, but its kernel carries four inlined copies
+  // of fc3 and spills: six fringe-heavy triangle patterns on RMAT-20 took 31 s
+  // in passes of four and two against 20 s one by one.
+  for (const auto& t : tris) {
     TriSet ts;
     memset(&ts, 0, sizeof(ts));
-    TriParams shared = tris[b].second;
-    for (size_t i = b; i < std::min(tris.size(), b + kTriFuse); i++) {
-      const int q = ts.np++;
-      const TriParams& tp = tris[i].second;
-      ts.sum1[q] = tp.sum1; ts.sum2[q] = tp.sum2; ts.sum3[q] = tp.sum3;
-      ts.rot[q] = tp.rot;
-      ts.slot[q] = tris[i].first->d_slot;
-      shared.sum1 = std::min(shared.sum1, tp.sum1);
-    }
-    st = ts.np == 1 ? launch_triangle_set<1, u64>(G, gv, shared, ts, s, launches, work)
-                    : launch_triangle_set<kTriFuse, u64>(G, gv, shared, ts, s, launches, work);
+    const TriParams& tp = t.second;
+    ts.np = 1;
+    ts.sum1[0] = tp.sum1; ts.sum2[0] = tp.sum2; ts.sum3[0] = tp.sum3;
+    ts.rot[0] = tp.rot;
+    ts.slot[0] = t.first->d_slot;
+    st = launch_triangle_set<1, u64>(G, gv, tp, ts, s, launches, work);
     if (st != FSGC_OK) return st;
   }
   for (CountJob* jp : single) {
