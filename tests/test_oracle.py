@@ -130,3 +130,41 @@ def test_fc3_counts_placements():
             continue
         venn = [0] + [rng.randint(0, 4) for _ in range(7)]
         assert oracle.fc3(fr, venn) == fc3_brute(fr, venn), (fr, venn)
+
+
+def test_oracle_matches_bruteforce_on_mixed_draws():
+    """Patterns drawn as the mixed-pattern workloads draw them (every core
+    shape, fringes on random nonempty core subsets), up to 8 vertices so that
+    the enumerator stays fast: the oracle's exact-placement count equals brute
+    force on small graphs, and its reference-semantics count equals it for
+    cores of at most three vertices."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from bench import CORE_SHAPES
+    rng = random.Random(20251210)
+    graphs = [fsgc.gen_er(14, 40, 21), fsgc.gen_rmat(5, 4, seed=22), fsgc.gen_chung_lu(24, 5.0, 2.3, 23)]
+    shapes = sorted(CORE_SHAPES)
+    seen = {}
+    while len(seen) < 150:
+        k, core = CORE_SHAPES[rng.choice(shapes)]
+        nf = rng.randint(0, 8 - k)
+        edges = list(core)
+        for i in range(nf):
+            sub = rng.randrange(1, 1 << k)
+            edges += [(j, k + i) for j in range(k) if sub >> j & 1]
+        try:
+            mo = fsgc.preprocess(k + nf, edges).to_bytes()
+        except fsgc.FsgcError:
+            continue
+        seen[mo] = (k + nf, edges)
+    cores = set()
+    for mo, (n, edges) in seen.items():
+        cores.add(mo[0])
+        for g in graphs:
+            b, _ = oracle.bruteforce(g.nindex, g.nlist, n, edges)
+            o = oracle.count(g.nindex, g.nlist, mo, exact_placements=True)
+            assert o["count"] == b, (n, edges, o, b)
+            if mo[0] <= 3:
+                assert oracle.count(g.nindex, g.nlist, mo)["count"] == b, (n, edges)
+    assert {1, 2, 3, 4, 5} <= cores  # vertex, edge, three-, four- and five-vertex cores
