@@ -343,8 +343,8 @@ int fsgc_server_stats_get(fsgc_server* srv, fsgc_server_stats* out);
  * valid for the life of the device's primary context: do not call this after
  * a cudaDeviceReset on that device.  Each call reads the graph's maximum degree
  * back to the host and waits for `stream` to finish the count before it
- * returns.  All calls share the array, so calls that overlap on the GPU race:
- * serialise them. */
+ * returns, so no call can be captured into a CUDA graph.  All calls share the
+ * array, so calls that overlap on the GPU race: serialise them. */
 int fsgc_count_wedge_noalloc(int n, int64_t m, const int64_t* d_nindex, const int32_t* d_nlist,
                              const fsgc_matching_order* mo, void* stream, fsgc_result* out, char* errbuf,
                              int errlen);
