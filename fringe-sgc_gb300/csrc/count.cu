@@ -8,9 +8,13 @@
 //   vertex core   one pass over the degrees;
 //   edge core     one pass over oriented edges, common-neighbour counts taken
 //                 from the loader's per-edge triangle supports;
-//   triangle core triangles enumerated once on the oriented graph, pairwise
-//                 overlaps from the supports, the triple overlap by a
-//                 warp-cooperative intersection over the smallest list;
+//   triangle core one block per lowest vertex a builds bitmap rows
+//                 N(a) & N(b_i) over the positions of N(a): the triangles are
+//                 the set bits, pairwise overlaps come from the supports and
+//                 the triple overlap is a popcount of two rows (the 4-clique
+//                 modes, and graphs whose out-lists would not fit in shared
+//                 memory, enumerate triangles on the oriented graph and take
+//                 the triple overlap by a warp-cooperative intersection);
 //   wedge core    (centre without fringes) aggregated per endpoint pair: the
 //                 reference evaluates the same formula once per centre, and
 //                 the formula does not depend on the centre, so each pair is
