@@ -138,3 +138,77 @@ def test_reference_arm_unavailable_without_the_cubin(monkeypatch, capsys):
     bench.main()
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and "unavailable" in line
+
+
+class _CountingCtx:
+    """fsgc.Context stand-in for the mixed workload: a count's result is a
+    function of the pattern bytes, so single counts and sets agree."""
+
+    launches = 0
+
+    def __init__(self, *_):
+        self.tuning = fsgc.Tuning.default()
+
+    def upload(self, g):
+        return 7
+
+    def prepare(self, gid):
+        pass
+
+    def set_tuning(self, t=None, **kw):
+        pass
+
+    def get_tuning(self):
+        return self.tuning
+
+    def _res(self, mo):
+        b = mo.to_bytes()
+
+        class R:
+            count = sum(b) * 1000003
+            raw_total = count
+            automorphisms = 1
+            core_type = min(mo.nodes, 5)
+            flags = 0
+            device_ms = 0.5
+        return R()
+
+    def count(self, gid, mo):
+        self.launches += 1
+        return self._res(mo)
+
+    def count_set(self, gid, mos):
+        self.launches += 1
+        return [self._res(mo) for mo in mos]
+
+    def synchronize(self):
+        pass
+
+    def release(self, gid):
+        pass
+
+    def close(self):
+        pass
+
+
+def test_mixed_line_splits_patterns_and_reports_both_modes(monkeypatch, capsys):
+    """The mixed workload's line: patterns without per-match work on the main
+    graph, general cores and fringed-centre wedges on the small one, both modes
+    timed, every batched count checked against its single count."""
+    monkeypatch.setattr(fsgc, "Context", _CountingCtx)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--workload", "mixed", "--mixed-patterns", "16",
+                                      "--mixed-scale", "8", "--general-scale", "5", "--steps", "1", "--warmup", "2"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    main, gen = line["config"]["main"], line["config"]["general"]
+    assert main["scale"] == 8 and main["patterns"] + (gen["patterns"] if gen else 0) == 16
+    assert not main["not_timed"]
+    assert line["value"] == main["batched_queries_per_s"] > 0
+    assert line["one_query_per_launch"]["value"] == main["single_queries_per_s"]
+    assert line["batched_over_single"] == main["batched_over_single"]
+    pats = dict(bench.draw_patterns(16, 20251208, max_core=6))
+    for name in main["single_per_pattern_ms"]:
+        assert not bench.per_match_family(pats[name])
+    if gen:
+        for name in gen["single_per_pattern_ms"]:
+            assert bench.per_match_family(pats[name])
