@@ -806,7 +806,8 @@ def main():
                          "listed, not timed")
     ap.add_argument("--mixed-budget", type=float, default=600.0,
                     help="mixed: seconds of single counts on the main graph; patterns beyond it are listed, "
-                         "not timed")
+                         "not timed (the kept patterns are then counted once more singly and max(2, warmup) "
+                         "+ steps times as a set, so the run takes up to about (3 + warmup + steps) x this)")
     ap.add_argument("--graphs", type=int, default=256, help="packed: member graphs")
     ap.add_argument("--nmax", type=int, default=50000, help="packed: largest member size")
     ap.add_argument("--serve-scales", default="6,7,8,9,10,11,12,13", help="serve: RMAT scales")
