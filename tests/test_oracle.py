@@ -168,3 +168,31 @@ def test_oracle_matches_bruteforce_on_mixed_draws():
             if mo[0] <= 3:
                 assert oracle.count(g.nindex, g.nlist, mo)["count"] == b, (n, edges)
     assert {1, 2, 3, 4, 5} <= cores  # vertex, edge, three-, four- and five-vertex cores
+
+
+def test_oracle_reproduces_the_reference_kernels_recorded_counts():
+    """tests/golden/reference_rmat16.json holds what the reference's own
+    kernels computed on the benchmark's RMAT-16 graph (count, raw total,
+    divisor, core type).  The oracle reproduces the five light patterns here;
+    the three heavy ones take minutes each on the CPU and are compared on the
+    GPU path instead."""
+    import json
+    import os
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    with open(os.path.join(root, "tests", "golden", "reference_rmat16.json")) as f:
+        rec = json.load(f)["patterns"]
+    R = bench.RMAT
+    g = fsgc.gen_rmat(16, R["edge_factor"], R["a"], R["b"], R["c"], R["seed"])
+    heavy = {"wedge_1_on_each_end", "4cycle_opposite", "4clique_3_distinct"}
+    checked = 0
+    for name, mo in bench.matching_orders():
+        if name in heavy:
+            continue
+        o = oracle.count(g.nindex, g.nlist, mo.to_bytes())
+        r = rec[name]
+        assert (o["count"], o["raw"], o["aut"], o["core"]) == (int(r["count"]), int(r["raw"]), r["aut"], r["core"]), name
+        checked += 1
+    assert checked == 5
